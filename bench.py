@@ -1,0 +1,433 @@
+"""Benchmark of the SLQ log-determinant path (one JSON line on stdout).
+
+Workload (default): the dense RBF kernel log-determinant of n = 16384 points
+x ~ U[0, 1]^3, K = exp(-|x_i - x_j|^2 / (2 * 0.2^2)) + 1e-2 I, Lanczos depth
+k = 64, p = 256 Rademacher probes, operator stored as a bf16 hi/lo split and
+applied with the three-term split product on the tensor cores.  One step is
+one complete log-determinant solve: build K from the points, draw the probes,
+run the batched Arnoldi/CGS2 iteration, the tridiagonal eigensolves and the
+quadrature, and average.  Inputs (operator 1.07 GB, Krylov basis 1.07 GB)
+are larger than L2, so no flush is needed between steps.
+
+--impl reference times the float64 NumPy restatement of matfree's algorithm
+(the oracle; matfree itself is JAX and cannot run here) on the host cores on
+a bounded probe sample of the same workload.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+CONFIGS = {
+    # name: (kind, n, k, p)
+    "rbf16k": ("rbf", 16384, 64, 256),
+    "dense1k": ("dense", 1000, 30, 100),
+    "laplace1m": ("csr", 1024 * 1024, 100, 64),
+}
+METRIC = "logdet solves/s"
+UNIT = "solves/s"
+
+
+def _peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return {"hbm": float(d["hbm_gbs"]), "tensor_burst": float(d["bf16_tflops"]),
+                "tensor_sustained": float(d["bf16_tflops_sustained"]), "source": "measured"}
+    except Exception:
+        return {"hbm": 6800.0, "tensor_burst": 1900.0, "tensor_sustained": 1700.0, "source": "fallback"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu_index = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu_index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+# --------------------------------------------------------------------------
+# GPU arm
+# --------------------------------------------------------------------------
+
+
+def _dist_init(n_gpus):
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    return rank, world, local
+
+
+def _barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def _max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def build_problem(cfg, seed=0):
+    """Host-side inputs of one solve (same seeds for both arms)."""
+    kind, n, k, p = CONFIGS[cfg]
+    if kind == "rbf":
+        x = np.random.default_rng(seed).uniform(0.0, 1.0, size=(n, 3)).astype(np.float32)
+        return {"kind": kind, "n": n, "k": k, "p": p, "x": x, "s2": 1.0, "ell": 0.2, "tau": 1e-2}
+    if kind == "dense":
+        B = np.random.default_rng(seed).standard_normal((n, n))
+        return {"kind": kind, "n": n, "k": k, "p": p, "A": (B @ B.T / n + np.eye(n)).astype(np.float32)}
+    m = int(round(math.sqrt(n)))
+    import scipy.sparse as sp
+
+    main = np.full(n, 4.0 + 0.1)
+    side = -np.ones(n - 1)
+    side[np.arange(1, n) % m == 0] = 0.0
+    ud = -np.ones(n - m)
+    A = sp.diags([main, side, side, ud, ud], [0, -1, 1, -m, m], format="csr")
+    A.eliminate_zeros()
+    A.sort_indices()
+    return {"kind": kind, "n": n, "k": k, "p": p, "csr": A}
+
+
+def gpu_arm(args):
+    import torch
+
+    import matfree_gb300 as mf
+    from matfree_gb300 import _lib
+    from matfree_gb300.funm import slq_values
+
+    rank, world, local = _dist_init(args.gpus)
+    prob = build_problem(args.config)
+    kind, n, k, p = prob["kind"], prob["n"], prob["k"], prob["p"]
+    precision = args.precision
+    dev = torch.device("cuda", torch.cuda.current_device())
+    key = mf.prng.prng_key(1 + rank)
+    mean_sem = torch.zeros(2, dtype=torch.float64, device=dev)
+
+    if kind == "rbf":
+        x_host = torch.from_numpy(prob["x"]).pin_memory()
+        x_dev = x_host.to(dev)
+        static = None
+    elif kind == "dense":
+        static = mf.DenseOperator(torch.from_numpy(prob["A"]).to(dev), precision=precision)
+        x_host = x_dev = None
+    else:
+        static = mf.CSROperator.from_scipy(prob["csr"], device=dev)
+        x_host = x_dev = None
+    sampler = mf.stochtrace.sampler_signs(torch.ones(n, device=dev), num=p)
+
+    def solve(x):
+        if kind == "rbf":
+            op = mf.RBFKernelOperator(x, s2=prob["s2"], ell=prob["ell"], tau=prob["tau"], precision=precision)
+        else:
+            op = static
+        V = sampler(key)
+        return slq_values(op, k, V, _lib.MFG_FUN_LOG, 0.0, mean_sem=mean_sem)
+
+    # warm-up
+    for _ in range(args.warmup):
+        solve(x_dev)
+    torch.cuda.synchronize()
+
+    # timed region: device-resident inputs, per-step events, launch accounting
+    lib = _lib.lib()
+    lib.mfg_profile_enable(1)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    _barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record()
+        for i in range(args.steps):
+            starts[i].record()
+            values = solve(x_dev)
+            ends[i].record()
+        t1.record()
+        torch.cuda.synchronize()
+        _barrier(world)
+    clocks = clk.summary()
+    total_ms = _max_over_ranks(t0.elapsed_time(t1), world)
+    step_ms = sorted(s.elapsed_time(e) for s, e in zip(starts, ends))
+    nc = len(_lib.PROF_CLASSES)
+    ms = (ctypes_arr := __import__("ctypes").c_double * nc)()
+    by = ctypes_arr()
+    fl = ctypes_arr()
+    ln = (__import__("ctypes").c_int64 * nc)()
+    _lib.check(lib.mfg_profile_read(nc, ms, by, fl, ln), "mfg_profile_read")
+    lib.mfg_profile_enable(0)
+    prof = {c: {"ms": ms[i], "bytes": by[i], "flops": fl[i], "launches": int(ln[i])}
+            for i, c in enumerate(_lib.PROF_CLASSES)}
+    est = float(mean_sem[0].item())
+
+    # end to end through the public API: host points in, scalar out
+    e2e = None
+    if kind == "rbf":
+        torch.cuda.synchronize()
+        _barrier(world)
+        t_start = time.perf_counter()
+        for _ in range(args.steps):
+            xd = x_host.to(dev, non_blocking=True)
+            solve(xd)
+            _ = float(mean_sem[0].item())
+        e2e_s = _max_over_ranks(time.perf_counter() - t_start, world)
+        e2e = {"value": world * args.steps / e2e_s, "unit": UNIT,
+               "h2d_bytes_per_step": int(x_host.numel() * 4), "d2h_bytes_per_step": 8}
+
+    result = {"rank": rank, "world": world, "total_ms": total_ms, "step_ms": step_ms, "prof": prof,
+              "clocks": clocks, "estimate": est, "e2e": e2e, "values": values, "key": key}
+    return result, prob
+
+
+def roofline(prof, peaks, steps):
+    """The class with the largest time share; HBM- or tensor-bound by its class."""
+    total = sum(v["ms"] for v in prof.values()) or 1.0
+    shares = {c: v["ms"] / total for c, v in prof.items()}
+    reortho_ms = prof["proj"]["ms"] + prof["sub"]["ms"]
+    reortho_b = prof["proj"]["bytes"] + prof["sub"]["bytes"]
+    apply_ms = prof["apply"]["ms"]
+    launches_reortho = prof["proj"]["launches"] + prof["sub"]["launches"]
+    if reortho_ms >= apply_ms:
+        per_launch_b = reortho_b / max(launches_reortho, 1)
+        per_launch_s = reortho_ms / 1e3 / max(launches_reortho, 1)
+        achieved = per_launch_b / per_launch_s / 1e9
+        return {"kernel": "cgs2 reortho (proj + sub)", "bound": "hbm", "achieved": achieved,
+                "peak": peaks["hbm"], "unit": "GB/s", "frac": achieved / peaks["hbm"],
+                "traffic": None, "time_share": (prof["proj"]["ms"] + prof["sub"]["ms"]) / total,
+                "launches": launches_reortho, "shares": shares}
+    fl = prof["apply"]["flops"]
+    launches = max(prof["apply"]["launches"], 1)
+    if fl > 0:
+        achieved = (fl / launches) / (apply_ms / 1e3 / launches) / 1e12
+        peak = peaks["tensor_sustained"]
+        return {"kernel": "operator apply", "bound": "tensor", "achieved": achieved, "peak": peak,
+                "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                "time_share": apply_ms / total, "launches": launches, "shares": shares}
+    b = prof["apply"]["bytes"]
+    achieved = (b / launches) / (apply_ms / 1e3 / launches) / 1e9
+    return {"kernel": "operator apply", "bound": "hbm", "achieved": achieved, "peak": peaks["hbm"],
+            "unit": "GB/s", "frac": achieved / peaks["hbm"], "traffic": None,
+            "time_share": apply_ms / total, "launches": launches, "shares": shares}
+
+
+# --------------------------------------------------------------------------
+# CPU arm (oracle restatement of matfree's algorithm, float64)
+# --------------------------------------------------------------------------
+
+
+def cpu_sample(prob, probes):
+    """float64 SLQ of the given probe rows; returns (values, seconds, build seconds)."""
+    from oracle import problems, slq
+
+    t0 = time.perf_counter()
+    if prob["kind"] == "rbf":
+        K = problems.rbf_kernel(prob["x"].astype(np.float64), prob["s2"], prob["ell"], 0.0)
+        K[np.diag_indices_from(K)] += prob["tau"]
+
+        def matmat(X):
+            return X @ K
+
+    elif prob["kind"] == "dense":
+        A = prob["A"].astype(np.float64)
+
+        def matmat(X):
+            return X @ A.T
+
+    else:
+        A = prob["csr"].astype(np.float64)
+
+        def matmat(X):
+            return (A @ X.T).T
+
+    t1 = time.perf_counter()
+    vals = slq.slq_batched(matmat, prob["k"], probes)
+    t2 = time.perf_counter()
+    return vals, t2 - t0, t1 - t0
+
+
+def cpu_probe_sample(prob, key, num):
+    from oracle import philox
+
+    return philox.rademacher(key, num, prob["n"])[:num]
+
+
+def reference_arm(args):
+    import torch  # noqa: F401  (only for rank discovery parity)
+
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return None
+    import matfree_gb300.prng as prng_host
+
+    prob = build_problem(args.config)
+    num = args.cpu_probes
+    key = prng_host.prng_key(1)
+    probes = cpu_probe_sample(prob, key, num)
+    rates = []
+    for i in range(args.warmup + args.steps):
+        _, secs, build = cpu_sample(prob, probes)
+        full = build + (secs - build) * prob["p"] / num
+        if i >= args.warmup:
+            rates.append(1.0 / full)
+    value = statistics.median(rates)
+    cores = len(os.sched_getaffinity(0))
+    return {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / value,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": _config(args),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{num} of {prob['p']} probes per step at full n and k; "
+                                       "operator build + per-probe time extrapolated to all probes; "
+                                       "float64 NumPy/OpenBLAS restatement of matfree's algorithm"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def _config(args):
+    kind, n, k, p = CONFIGS[args.config]
+    desc = {"rbf": "dense RBF kernel log-det (x~U[0,1]^3, ell=0.2, tau=1e-2)",
+            "dense": "dense SPD B B^T/n + I log-det", "csr": "5-point Laplacian + 0.1 I log-det (CSR)"}[kind]
+    return {"workload": f"{desc}, n={n}, k={k}, p={p} Rademacher probes, operator {args.precision}",
+            "n": n, "k": k, "p": p, "precision": args.precision, "parallelism": "replicas",
+            "l2": "inputs larger than L2 (operator and Krylov basis > 129 MB); no flush"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="rbf16k", choices=sorted(CONFIGS))
+    ap.add_argument("--precision", default="bf16x3", choices=["fp32", "bf16", "bf16x3", "fp64"])
+    ap.add_argument("--cpu-probes", type=int, default=8)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+
+    if args.impl == "reference":
+        line = reference_arm(args)
+        if line is not None:
+            print(json.dumps(line), flush=True)
+        return
+
+    res, prob = gpu_arm(args)
+    if res["rank"] != 0:
+        return
+    world = res["world"]
+    peaks = _peaks()
+    value = world * args.steps / (res["total_ms"] / 1e3)
+    rl = roofline(res["prof"], peaks, args.steps)
+    rl["peak_source"] = f"of {peaks['source']}"
+    launches = sum(v["launches"] for v in res["prof"].values())
+    step_ms = res["step_ms"]
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": res["total_ms"] / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 basis / bf16x3 operator / f64 reductions"
+        if args.precision == "bf16x3" else args.precision, "data": "synthetic (seeded)",
+        "config": _config(args),
+        "latency_ms": {"p50": step_ms[len(step_ms) // 2], "p99": step_ms[min(len(step_ms) - 1, int(0.99 * len(step_ms)))]},
+        "estimate": res["estimate"], "roofline": rl, "gpu_launches": launches,
+        "clocks": res["clocks"], "e2e": res["e2e"],
+        "kernel_ms_per_step": {c: v["ms"] / args.steps for c, v in res["prof"].items()},
+    }
+    if not args.no_cpu_baseline:
+        num = args.cpu_probes
+        probes = cpu_probe_sample(prob, res["key"], num)
+        vals, secs, build = cpu_sample(prob, probes)
+        full = build + (secs - build) * prob["p"] / num
+        gpu_vals = res["values"][:num].cpu().numpy()
+        rel = float(abs(gpu_vals.mean() - vals.mean()) / abs(vals.mean()))
+        line["cpu_baseline"] = {
+            "value": 1.0 / full, "unit": UNIT, "cores": len(os.sched_getaffinity(0)), "kind": "port",
+            "sample": f"{num} of {prob['p']} probes at full n and k (float64 NumPy restatement, "
+                      f"{secs:.1f} s incl. {build:.1f} s operator build); extrapolated linearly in probes"}
+        line["rel_err_vs_fp64"] = {"value": rel, "on": f"mean over the first {num} probes, identical probe vectors"}
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,189 @@
+/*
+ * matfree_gb300 — C ABI of the GB300 (sm_103a) stochastic Lanczos quadrature path.
+ *
+ * Every entry point takes plain device pointers, sizes and a CUDA stream
+ * (passed as void*; NULL is the legacy default stream), returns an int status
+ * (MFG_OK == 0) and allocates no device memory: the caller owns every buffer,
+ * including the workspace whose size mfg_slq_workspace_bytes() reports.
+ * Calls on different streams with different workspaces may run concurrently.
+ *
+ * Memory layout ("probe-major panels"): a set of p vectors of length n is
+ * stored as p rows of ld elements (ld >= n, ld % 8 == 0, 16-byte aligned
+ * base).  The Krylov basis of p probes with k vectors each is p x k rows of ld
+ * elements (probe b, vector i at row b*k + i).  Hessenberg matrices are p
+ * row-major k x k float64 blocks (column j holds step j's projection
+ * coefficients and, below the diagonal, the norm of the new vector).
+ *
+ * The reference (pnkraemer/matfree) is JAX; the functions each entry point
+ * stands in for are cited file:line relative to that project.
+ */
+#ifndef MATFREE_GB300_H
+#define MATFREE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define MFG_API __attribute__((visibility("default")))
+#else
+#define MFG_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+  MFG_OK = 0,
+  MFG_ERR_BAD_ARG = 1,     /* a size, pointer, alignment or flag is invalid   */
+  MFG_ERR_RANGE = 2,       /* num_matvecs outside [0, n] ("exceeds")          */
+  MFG_ERR_WORKSPACE = 3,   /* workspace smaller than mfg_slq_workspace_bytes  */
+  MFG_ERR_CUDA = 4,        /* a CUDA runtime/driver call failed               */
+  MFG_ERR_UNSUPPORTED = 5, /* combination not implemented (e.g. op/precision) */
+  MFG_ERR_NO_CONVERGENCE = 6 /* tridiagonal eigensolver hit its sweep limit   */
+};
+
+/* ---- element type of vectors and bases --------------------------------- */
+enum { MFG_F32 = 0, MFG_F64 = 1 };
+
+/* ---- operator descriptors ---------------------------------------------- */
+enum {
+  MFG_OP_DENSE = 0,    /* row-major n x n matrix, see precision below          */
+  MFG_OP_CSR = 1,      /* CSR, int32 row_ptr/col_idx, float32 values           */
+  MFG_OP_CALLBACK = 2  /* caller-supplied apply(V -> W) on device panels        */
+};
+
+enum {
+  MFG_PREC_FP32 = 0,   /* dense float32 matrix, float32 CUDA-core product      */
+  MFG_PREC_BF16 = 1,   /* dense bf16 matrix (a), tcgen05 bf16 x bf16 -> fp32   */
+  MFG_PREC_BF16X3 = 2, /* bf16 hi (a) + lo (a_lo); hi*hi + hi*lo + lo*hi       */
+  MFG_PREC_FP64 = 3    /* dense float64 matrix and float64 basis               */
+};
+
+/* W = A V for a probe-major panel V (p rows of ld), all on `stream`. */
+typedef int (*mfg_apply_fn)(void *ctx, const void *V, void *W, int64_t n,
+                            int64_t p, int64_t ld, void *stream);
+
+typedef struct mfg_operator {
+  int32_t kind;      /* MFG_OP_*                                              */
+  int32_t precision; /* MFG_PREC_* (dense); MFG_PREC_FP32 for CSR/callback    */
+  int64_t n;         /* dimension                                             */
+  const void *a;     /* dense: matrix (fp32/fp64/bf16-hi), lda elements/row   */
+  const void *a_lo;  /* dense BF16X3: bf16 low part, same lda                 */
+  int64_t lda;
+  const int32_t *row_ptr; /* CSR: n + 1 entries                               */
+  const int32_t *col_idx; /* CSR: nnz entries                                 */
+  const float *values;    /* CSR: nnz entries                                 */
+  int64_t nnz;
+  double shift;      /* the operator applied is A + shift * I                 */
+  mfg_apply_fn apply;/* callback operators                                    */
+  void *ctx;
+} mfg_operator;
+
+/* ---- matrix functions of the quadrature -------------------------------- */
+enum {
+  MFG_FUN_LOG = 0,  /* f(x) = log(x)                        (funm.py:199)    */
+  MFG_FUN_EXP = 1,  /* f(x) = exp(param * x)                                 */
+  MFG_FUN_POW = 2,  /* f(x) = x ** param                                     */
+  MFG_FUN_NONE = 3  /* eigenvalues and first components only                 */
+};
+
+/* Library version (major*10000 + minor*100 + patch). */
+MFG_API int mfg_version(void);
+
+/* Human-readable text of a status code; never NULL. */
+MFG_API const char *mfg_status_string(int status);
+
+/* Bytes of workspace the SLQ / tridiagonalisation entry points need. */
+MFG_API size_t mfg_slq_workspace_bytes(const mfg_operator *op, int64_t k, int64_t p, int64_t ld);
+
+/* Probe sampler: Rademacher +-1 (Philox4x32-10, key = 2 words) written as a
+ * probe-major panel of `dtype` (MFG_F32/MFG_F64); padding columns set to 0.
+ * Replaces stochtrace.sampler_signs (matfree/stochtrace.py:932-937,974-977)
+ * and backend/prng.py:26-29. */
+MFG_API int mfg_sampler_signs(const uint32_t key[2], int64_t num, int64_t n, int64_t ld,
+                      int32_t dtype, void *out, void *stream);
+
+/* Probe sampler: standard normal (Box-Muller on Philox words).
+ * Replaces stochtrace.sampler_normal (matfree/stochtrace.py:927-929). */
+MFG_API int mfg_sampler_normal(const uint32_t key[2], int64_t num, int64_t n, int64_t ld,
+                       int32_t dtype, void *out, void *stream);
+
+/* W = (A + shift I) V for a probe-major panel; the batched `matvec(v)` that
+ * matfree evaluates under vmap (matfree/decomp.py:460, stochtrace.py:49). */
+MFG_API int mfg_operator_apply(const mfg_operator *op, const void *V, void *W, int64_t p,
+                       int64_t ld, void *workspace, size_t workspace_bytes, void *stream);
+
+/* Batched Arnoldi with classical Gram-Schmidt applied twice over the p
+ * columns of V (probe-major, dtype F64 for MFG_PREC_FP64 else F32):
+ * Q (p*k rows of ld), H (p k x k float64), residual (p rows of ld) and
+ * init_len_inv[p] = 1/||v_b||.
+ * Replaces decomp.tridiag_sym(k, reortho="full") / decomp.hessenberg
+ * (matfree/decomp.py:30-152, 353-477).  reortho: 1 = "full", 0 = "none". */
+MFG_API int mfg_hessenberg(const mfg_operator *op, int64_t k, int64_t p, const void *V,
+                   int64_t ld, int32_t reortho, void *Q, double *H, void *residual,
+                   double *init_len_inv, void *workspace, size_t workspace_bytes,
+                   void *stream);
+
+/* For each of p Hessenberg matrices: T = (H + H^T)/2 restricted to its
+ * tridiagonal part, eigenvalues by implicit QL in float64 with the first
+ * eigenvector components tracked (Golub-Welsch), and
+ * values[b] = scale[b] * sum_i f(lambda_i) s_1i^2.  eigvals / first_sq may be
+ * NULL; scale may be NULL (1).
+ * Replaces funm.dense_funm_sym_eigh + the quadform's e1^T f(T) e1
+ * (matfree/funm.py:239-241, 322-335) and decomp.py:133-135. */
+MFG_API int mfg_tridiag_quadrature(int64_t k, int64_t p, const double *H, int32_t fun,
+                           double param, const double *scale, double *values,
+                           double *eigvals, double *first_sq, void *stream);
+
+/* The whole SLQ integrand for p probes: ||v_b||^2 e1^T f(T_b) e1 with
+ * T_b from mfg_hessenberg(reortho="full") of v_b/||v_b||.  values[p] and
+ * mean_sem[2] = (mean, std/sqrt(p)) are device float64 (mean_sem may be NULL).
+ * Replaces estimator_monte_carlo(monte_carlo_funm_sym(dense_funm_sym_eigh(f),
+ * tridiag_sym(k)), sampler) (matfree/stochtrace.py:47-50,82-87;
+ * funm.py:186-241).  Q, H may be NULL: the basis then lives in the workspace
+ * and is not returned. */
+MFG_API int mfg_slq(const mfg_operator *op, int64_t k, int64_t p, const void *probes,
+            int64_t ld, int32_t fun, double param, double *values, double *mean_sem,
+            void *Q, double *H, void *workspace, size_t workspace_bytes, void *stream);
+
+/* Dense RBF kernel matrix K_ij = s2 exp(-|x_i - x_j|^2 / (2 ell^2)) from
+ * points x (n x dim float32, row-major), WITHOUT the nugget (pass tau as the
+ * operator shift).  precision selects the storage: FP32 -> a (float),
+ * BF16 -> a (bf16), BF16X3 -> a (bf16 hi) and a_lo (bf16 lo), FP64 -> a
+ * (double).  Stands in for the user covariance closure of
+ * tutorials/8_gaussian_logpdf.py:21-30. */
+MFG_API int mfg_rbf_build(const float *x, int64_t n, int32_t dim, double s2, double ell,
+                  int32_t precision, void *a, void *a_lo, int64_t lda, void *stream);
+
+/* Split a float32 matrix into bf16 hi = bf16(a) and lo = bf16(a - hi). */
+/* ---- launch accounting (diagnostics) ------------------------------------ */
+enum {
+  MFG_PROF_APPLY = 0,  /* operator application (GEMM / SpMM / callback)        */
+  MFG_PROF_PROJ = 1,   /* Gram-Schmidt projections Q^T w                        */
+  MFG_PROF_SUB = 2,    /* Gram-Schmidt updates w -= Q h (and norms)             */
+  MFG_PROF_SCALE = 3,  /* normalisation (+ bf16 split of the new vector)        */
+  MFG_PROF_QUAD = 4,   /* tridiagonal eigensolve + quadrature + mean            */
+  MFG_PROF_OTHER = 5,  /* samplers, operator builds, initial norms              */
+  MFG_PROF_CLASSES = 6
+};
+
+/* Reset the process-wide launch counters; timing != 0 also brackets every
+ * launch with CUDA events on its stream (for benchmarks; not thread-safe with
+ * respect to concurrent readers). */
+MFG_API int mfg_profile_enable(int timing);
+
+/* Per class: summed event time (ms), algorithmic bytes and flops of the timed
+ * launches, and the number of launches since the last reset.  Synchronises
+ * on the recorded events.  Any output pointer may be NULL. */
+MFG_API int mfg_profile_read(int32_t nclasses, double *ms, double *bytes, double *flops,
+                             int64_t *launches);
+
+MFG_API int mfg_split_bf16(const float *a, int64_t rows, int64_t cols, int64_t lda,
+                   void *hi, void *lo, int64_t ld_out, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MATFREE_GB300_H */

@@ -1,0 +1,502 @@
+// C entry points (include/matfree_gb300.h) and the batched Arnoldi driver.
+//
+// The driver issues, per Krylov step j, on the caller's stream:
+//   operator apply  W = A q_j            (tcgen05 GEMM / CUDA-core GEMM / SpMM / callback)
+//   projection      H[:, 0..j][j] = Q^T W          (first Gram-Schmidt pass)
+//   update          W -= Q H[:, j]
+//   projection      h2 = Q^T W                      (second pass, reortho = full)
+//   update + norm   W -= Q h2, beta = ||W||, H[j+1][j] = beta
+//   normalise       q_{j+1} = W / beta  (+ bf16 hi/lo copies for the tensor cores)
+// mirroring matfree/decomp.py:454-477 step by step, batched over the probes.
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace mfg {
+
+// ---------------------------------------------------------------------------
+// Launch accounting: every kernel the driver issues is counted per class; when
+// timing is on, a pair of CUDA events brackets each launch on its stream and
+// the launch's algorithmic bytes and flops are recorded with it.  Process-wide
+// and meant for benchmarks (one driver thread at a time).
+// ---------------------------------------------------------------------------
+
+struct ProfRec {
+  int cls;
+  size_t e0, e1;
+  double bytes, flops;
+};
+
+struct Profiler {
+  std::mutex mu;
+  bool timing = false;
+  std::vector<cudaEvent_t> pool;
+  size_t next = 0;
+  std::vector<ProfRec> recs;
+  int64_t launches[MFG_PROF_CLASSES] = {0};
+};
+
+static Profiler &prof() {
+  static Profiler p;
+  return p;
+}
+
+static size_t prof_begin(cudaStream_t s) {
+  Profiler &P = prof();
+  if (!P.timing) return (size_t)-1;
+  std::lock_guard<std::mutex> lk(P.mu);
+  while (P.pool.size() < P.next + 2) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) return (size_t)-1;
+    P.pool.push_back(e);
+  }
+  const size_t e0 = P.next;
+  P.next += 2;
+  cudaEventRecord(P.pool[e0], s);
+  return e0;
+}
+
+static void prof_end(size_t e0, int cls, double bytes, double flops, cudaStream_t s) {
+  Profiler &P = prof();
+  std::lock_guard<std::mutex> lk(P.mu);
+  P.launches[cls] += 1;
+  if (e0 == (size_t)-1) return;
+  cudaEventRecord(P.pool[e0 + 1], s);
+  P.recs.push_back(ProfRec{cls, e0, e0 + 1, bytes, flops});
+}
+
+#define MFG_LAUNCH(cls, bytes, flops, call)        \
+  do {                                             \
+    const size_t _e = prof_begin(s);               \
+    const int _st = (call);                        \
+    prof_end(_e, (cls), (bytes), (flops), s);      \
+    if (_st != MFG_OK) return _st;                 \
+  } while (0)
+
+struct WsLayout {
+  size_t w, panel, norm, len0, h2, partials, counters, status, hi, lo, q, h, values, eig, fsq, total;
+};
+
+static int elem_size_for(const mfg_operator *op) {
+  return op->precision == MFG_PREC_FP64 ? 8 : 4;
+}
+
+static bool uses_bf16(const mfg_operator *op) {
+  return op->kind == MFG_OP_DENSE &&
+         (op->precision == MFG_PREC_BF16 || op->precision == MFG_PREC_BF16X3);
+}
+
+static WsLayout layout(const mfg_operator *op, int64_t k, int64_t p, int64_t ld) {
+  WsLayout L{};
+  const size_t es = (size_t)elem_size_for(op);
+  const int64_t nch = es == 8 ? num_chunks<double>(op->n) : num_chunks<float>(op->n);
+  const int64_t kk = k > 0 ? k : 1;
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    const size_t o = off;
+    off = align_up(off + bytes, 256);
+    return o;
+  };
+  L.w = take((size_t)p * ld * es);
+  L.panel = take(op->kind == MFG_OP_CALLBACK ? (size_t)p * ld * es : 0);
+  L.norm = take((size_t)p * 8);
+  L.len0 = take((size_t)p * 8);
+  L.h2 = take((size_t)p * kk * 8);
+  L.partials = take((size_t)p * nch * (kk + 1) * 8);
+  L.counters = take((size_t)p * 4);
+  L.status = take(16);
+  L.hi = take(uses_bf16(op) ? (size_t)p * ld * 2 : 0);
+  L.lo = take(uses_bf16(op) && op->precision == MFG_PREC_BF16X3 ? (size_t)p * ld * 2 : 0);
+  L.q = take((size_t)p * kk * ld * es);
+  L.h = take((size_t)p * kk * kk * 8);
+  L.values = take((size_t)p * 8);
+  L.eig = take((size_t)p * kk * 8);
+  L.fsq = take((size_t)p * kk * 8);
+  L.total = off + 256;  // slack for aligning the caller's base pointer
+  return L;
+}
+
+static bool aligned16(const void *ptr) { return ((uintptr_t)ptr & 15u) == 0; }
+
+static int check_op(const mfg_operator *op) {
+  if (!op || op->n <= 0) return MFG_ERR_BAD_ARG;
+  switch (op->kind) {
+    case MFG_OP_DENSE:
+      if (!op->a || op->lda < op->n || op->lda % 8 != 0 || !aligned16(op->a)) return MFG_ERR_BAD_ARG;
+      if (op->precision == MFG_PREC_BF16X3 && (!op->a_lo || !aligned16(op->a_lo))) return MFG_ERR_BAD_ARG;
+      if (op->precision < MFG_PREC_FP32 || op->precision > MFG_PREC_FP64) return MFG_ERR_BAD_ARG;
+      return MFG_OK;
+    case MFG_OP_CSR:
+      if (!op->row_ptr || (op->nnz > 0 && (!op->col_idx || !op->values))) return MFG_ERR_BAD_ARG;
+      if (op->precision != MFG_PREC_FP32) return MFG_ERR_UNSUPPORTED;
+      return MFG_OK;
+    case MFG_OP_CALLBACK:
+      if (!op->apply) return MFG_ERR_BAD_ARG;
+      if (op->precision != MFG_PREC_FP32 && op->precision != MFG_PREC_FP64) return MFG_ERR_BAD_ARG;
+      return MFG_OK;
+    default:
+      return MFG_ERR_BAD_ARG;
+  }
+}
+
+static char *ws_base(void *workspace) {
+  return reinterpret_cast<char *>(align_up((size_t)workspace, 256));
+}
+
+// W (ld) = A V (ldv); vhi/vlo are the bf16 copies of V (ldvb) for the
+// tensor-core precisions, panel a contiguous scratch panel for callbacks.
+template <typename T>
+static int apply_op(const mfg_operator *op, const T *V, int64_t ldv, T *W, int64_t ldw, int64_t p,
+                    const __nv_bfloat16 *vhi, const __nv_bfloat16 *vlo, int64_t ldvb, T *panel,
+                    int *status, cudaStream_t s) {
+  const int64_t n = op->n;
+  switch (op->kind) {
+    case MFG_OP_DENSE:
+      if (op->precision == MFG_PREC_FP32 || op->precision == MFG_PREC_FP64)
+        return launch_dense_simt<T>(reinterpret_cast<const T *>(op->a), op->lda, V, ldv, W, ldw, n,
+                                    p, op->shift, s);
+      if constexpr (sizeof(T) == 4) {
+        const __nv_bfloat16 *alo =
+            op->precision == MFG_PREC_BF16X3 ? reinterpret_cast<const __nv_bfloat16 *>(op->a_lo) : nullptr;
+        return launch_dense_tcgen05(reinterpret_cast<const __nv_bfloat16 *>(op->a), alo, op->lda,
+                                    vhi, op->precision == MFG_PREC_BF16X3 ? vlo : nullptr, ldvb,
+                                    V, ldv, W, ldw, n, p, op->shift, status, s);
+      }
+      return MFG_ERR_UNSUPPORTED;
+    case MFG_OP_CSR:
+      if constexpr (sizeof(T) == 4)
+        return launch_csr_spmm(op->row_ptr, op->col_idx, op->values, n, V, ldv, W, ldw, p,
+                               op->shift, s);
+      return MFG_ERR_UNSUPPORTED;
+    case MFG_OP_CALLBACK: {
+      const T *src = V;
+      if (ldv != ldw) {
+        MFG_CUDA_TRY(cudaMemcpy2DAsync(panel, ldw * sizeof(T), V, ldv * sizeof(T), n * sizeof(T),
+                                       p, cudaMemcpyDeviceToDevice, s));
+        src = panel;
+      }
+      const int rc = op->apply(op->ctx, src, W, n, p, ldw, (void *)s);
+      if (rc != 0) return MFG_ERR_CUDA;
+      if (op->shift != 0.0) return MFG_ERR_UNSUPPORTED;  // callbacks fold their own shift
+      return MFG_OK;
+    }
+    default:
+      return MFG_ERR_BAD_ARG;
+  }
+}
+
+// Algorithmic bytes and flops of one operator application to p vectors.
+static void apply_cost(const mfg_operator *op, int64_t p, double *bytes, double *flops) {
+  const double n = (double)op->n, pp = (double)p;
+  const double vec_io = 2.0 * n * pp * 4.0;
+  switch (op->kind) {
+    case MFG_OP_DENSE: {
+      const double mats = op->precision == MFG_PREC_BF16X3 ? 2.0 : 1.0;
+      const double es = op->precision == MFG_PREC_FP64 ? 8.0 : (op->precision == MFG_PREC_FP32 ? 4.0 : 2.0);
+      *bytes = mats * n * n * es + vec_io * (op->precision == MFG_PREC_FP64 ? 2.0 : 1.0);
+      *flops = 2.0 * n * n * pp * (op->precision == MFG_PREC_BF16X3 ? 3.0 : 1.0);
+      return;
+    }
+    case MFG_OP_CSR:
+      *bytes = 8.0 * (double)op->nnz + 4.0 * (n + 1.0) + vec_io;
+      *flops = 2.0 * (double)op->nnz * pp;
+      return;
+    default:
+      *bytes = vec_io;
+      *flops = 0.0;
+  }
+}
+
+template <typename T>
+static int run_hessenberg(const mfg_operator *op, int64_t k, int64_t p, const T *V, int64_t ld,
+                          int reortho, T *Q, double *H, T *R, double *init_len_inv,
+                          const WsLayout &L, char *ws, cudaStream_t s) {
+  const int64_t n = op->n;
+  const double vecb = (double)n * (double)p * (double)sizeof(T);  // one panel
+  double ab = 0.0, af = 0.0;
+  apply_cost(op, p, &ab, &af);
+  T *Wb = reinterpret_cast<T *>(ws + L.w);
+  T *panel = reinterpret_cast<T *>(ws + L.panel);
+  double *norm = reinterpret_cast<double *>(ws + L.norm);
+  double *len0 = reinterpret_cast<double *>(ws + L.len0);
+  double *h2 = reinterpret_cast<double *>(ws + L.h2);
+  double *partials = reinterpret_cast<double *>(ws + L.partials);
+  unsigned *counters = reinterpret_cast<unsigned *>(ws + L.counters);
+  int *status = reinterpret_cast<int *>(ws + L.status);
+  __nv_bfloat16 *hi = uses_bf16(op) ? reinterpret_cast<__nv_bfloat16 *>(ws + L.hi) : nullptr;
+  __nv_bfloat16 *lo = (uses_bf16(op) && op->precision == MFG_PREC_BF16X3)
+                          ? reinterpret_cast<__nv_bfloat16 *>(ws + L.lo)
+                          : nullptr;
+  const int64_t qb = k * ld;  // probe stride of the basis
+
+  MFG_CUDA_TRY(cudaMemsetAsync(counters, 0, (size_t)p * 4, s));
+  MFG_CUDA_TRY(cudaMemsetAsync(status, 0, 16, s));
+  if (k > 0) MFG_CUDA_TRY(cudaMemsetAsync(H, 0, (size_t)p * k * k * 8, s));
+
+  const double bfb = hi ? (double)n * (double)p * 2.0 * (lo ? 2.0 : 1.0) : 0.0;
+
+  // initial length (decomp.py:436) -> 1 / length
+  MFG_LAUNCH(MFG_PROF_OTHER, vecb, 2.0 * vecb / sizeof(T),
+             launch_sub<T>(nullptr, 0, 0, 0, nullptr, 0, 0, V, nullptr, ld, n, p, true, false,
+                           partials, counters, len0, nullptr, 0, s));
+  if (init_len_inv) MFG_LAUNCH(MFG_PROF_OTHER, 16.0 * p, (double)p, launch_inv(len0, init_len_inv, p, s));
+  if (k == 0) {
+    if (R)
+      MFG_CUDA_TRY(cudaMemcpy2DAsync(R, ld * sizeof(T), V, ld * sizeof(T), ld * sizeof(T), p,
+                                     cudaMemcpyDeviceToDevice, s));
+    return MFG_OK;
+  }
+  MFG_LAUNCH(MFG_PROF_SCALE, 2.0 * vecb + bfb, vecb / sizeof(T),
+             launch_scale<T>(V, ld, n, p, len0, Q, qb, hi, lo, ld, s));
+
+  for (int64_t j = 0; j < k; ++j) {
+    const T *qj = Q + j * ld;
+    MFG_LAUNCH(MFG_PROF_APPLY, ab, af,
+               apply_op<T>(op, qj, qb, Wb, ld, p, hi, lo, ld, panel, status, s));
+    const int ncols = (int)(j + 1);
+    const double pb = (ncols + 1.0) * vecb, pf = 2.0 * ncols * vecb / sizeof(T);
+    const double ub = (ncols + 2.0) * vecb;
+    // first pass: h = Q^T w into column j of H
+    MFG_LAUNCH(MFG_PROF_PROJ, pb, pf,
+               launch_proj<T>(Q, qb, ld, ncols, Wb, ld, n, p, partials, counters, H + j, k * k, k, s));
+    const bool last = (j + 1 == k);
+    double *hsub = last ? nullptr : H + (j + 1) * k + j;
+    if (reortho) {
+      MFG_LAUNCH(MFG_PROF_SUB, ub, pf,
+                 launch_sub<T>(Q, qb, ld, ncols, H + j, k * k, k, Wb, Wb, ld, n, p, false, true,
+                               partials, counters, norm, nullptr, 0, s));
+      MFG_LAUNCH(MFG_PROF_PROJ, pb, pf,
+                 launch_proj<T>(Q, qb, ld, ncols, Wb, ld, n, p, partials, counters, h2, k, 1, s));
+      MFG_LAUNCH(MFG_PROF_SUB, ub, pf + 2.0 * vecb / sizeof(T),
+                 launch_sub<T>(Q, qb, ld, ncols, h2, k, 1, Wb, Wb, ld, n, p, true, true, partials,
+                               counters, norm, hsub, k * k, s));
+    } else {
+      MFG_LAUNCH(MFG_PROF_SUB, ub, pf + 2.0 * vecb / sizeof(T),
+                 launch_sub<T>(Q, qb, ld, ncols, H + j, k * k, k, Wb, Wb, ld, n, p, true, true,
+                               partials, counters, norm, hsub, k * k, s));
+    }
+    if (!last)
+      MFG_LAUNCH(MFG_PROF_SCALE, 2.0 * vecb + bfb, vecb / sizeof(T),
+                 launch_scale<T>(Wb, ld, n, p, norm, Q + (j + 1) * ld, qb, hi, lo, ld, s));
+  }
+  if (R)
+    MFG_CUDA_TRY(cudaMemcpy2DAsync(R, ld * sizeof(T), Wb, ld * sizeof(T), ld * sizeof(T), p,
+                                   cudaMemcpyDeviceToDevice, s));
+  return MFG_OK;
+}
+
+__global__ void square_kernel(const double *x, double *y, int64_t p) {
+  const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (b < p) y[b] = x[b] * x[b];
+}
+
+static int launch_square(const double *x, double *y, int64_t p, cudaStream_t s) {
+  square_kernel<<<(unsigned)ceil_div(p, 128), 128, 0, s>>>(x, y, p);
+  return cudaGetLastError() == cudaSuccess ? MFG_OK : MFG_ERR_CUDA;
+}
+
+}  // namespace mfg
+
+using namespace mfg;
+
+extern "C" {
+
+int mfg_version(void) { return 100; }
+
+int mfg_profile_enable(int timing) {
+  Profiler &P = prof();
+  std::lock_guard<std::mutex> lk(P.mu);
+  P.timing = timing != 0;
+  P.next = 0;
+  P.recs.clear();
+  for (int c = 0; c < MFG_PROF_CLASSES; ++c) P.launches[c] = 0;
+  return MFG_OK;
+}
+
+int mfg_profile_read(int32_t nclasses, double *ms, double *bytes, double *flops, int64_t *launches) {
+  if (nclasses <= 0 || nclasses > MFG_PROF_CLASSES) return MFG_ERR_BAD_ARG;
+  Profiler &P = prof();
+  std::lock_guard<std::mutex> lk(P.mu);
+  for (int c = 0; c < nclasses; ++c) {
+    if (ms) ms[c] = 0.0;
+    if (bytes) bytes[c] = 0.0;
+    if (flops) flops[c] = 0.0;
+    if (launches) launches[c] = P.launches[c];
+  }
+  for (const ProfRec &r : P.recs) {
+    if (r.cls >= nclasses) continue;
+    if (cudaEventSynchronize(P.pool[r.e1]) != cudaSuccess) return MFG_ERR_CUDA;
+    float t = 0.f;
+    if (cudaEventElapsedTime(&t, P.pool[r.e0], P.pool[r.e1]) != cudaSuccess) return MFG_ERR_CUDA;
+    if (ms) ms[r.cls] += t;
+    if (bytes) bytes[r.cls] += r.bytes;
+    if (flops) flops[r.cls] += r.flops;
+  }
+  return MFG_OK;
+}
+
+const char *mfg_status_string(int status) {
+  switch (status) {
+    case MFG_OK: return "ok";
+    case MFG_ERR_BAD_ARG: return "invalid argument";
+    case MFG_ERR_RANGE: return "num_matvecs exceeds the acceptable range";
+    case MFG_ERR_WORKSPACE: return "workspace too small";
+    case MFG_ERR_CUDA: return "CUDA error";
+    case MFG_ERR_UNSUPPORTED: return "unsupported operator/precision/shape";
+    case MFG_ERR_NO_CONVERGENCE: return "tridiagonal eigensolver did not converge";
+    default: return "unknown status";
+  }
+}
+
+size_t mfg_slq_workspace_bytes(const mfg_operator *op, int64_t k, int64_t p, int64_t ld) {
+  if (check_op(op) != MFG_OK || k < 0 || p <= 0 || ld < op->n) return 0;
+  return layout(op, k, p, ld).total;
+}
+
+static int check_panel(const mfg_operator *op, int64_t p, int64_t ld) {
+  if (p <= 0 || p > 65535 || ld < op->n || ld % 8 != 0) return MFG_ERR_BAD_ARG;
+  return MFG_OK;
+}
+
+int mfg_sampler_signs(const uint32_t key[2], int64_t num, int64_t n, int64_t ld, int32_t dtype,
+                      void *out, void *stream) {
+  if (!key || !out || n <= 0 || ld < n || ld % 8 != 0 || num < 0 || !aligned16(out))
+    return MFG_ERR_BAD_ARG;
+  cudaStream_t s = as_stream(stream);
+  const double b = (double)num * ld * (dtype == MFG_F64 ? 8.0 : 4.0);
+  if (dtype == MFG_F32)
+    MFG_LAUNCH(MFG_PROF_OTHER, b, 0.0, launch_sampler<float>(0, key[0], key[1], num, n, ld, (float *)out, s));
+  else if (dtype == MFG_F64)
+    MFG_LAUNCH(MFG_PROF_OTHER, b, 0.0, launch_sampler<double>(0, key[0], key[1], num, n, ld, (double *)out, s));
+  else
+    return MFG_ERR_BAD_ARG;
+  return MFG_OK;
+}
+
+int mfg_sampler_normal(const uint32_t key[2], int64_t num, int64_t n, int64_t ld, int32_t dtype,
+                       void *out, void *stream) {
+  if (!key || !out || n <= 0 || ld < n || ld % 8 != 0 || num < 0 || !aligned16(out))
+    return MFG_ERR_BAD_ARG;
+  cudaStream_t s = as_stream(stream);
+  const double b = (double)num * ld * (dtype == MFG_F64 ? 8.0 : 4.0);
+  if (dtype == MFG_F32)
+    MFG_LAUNCH(MFG_PROF_OTHER, b, 0.0, launch_sampler<float>(1, key[0], key[1], num, n, ld, (float *)out, s));
+  else if (dtype == MFG_F64)
+    MFG_LAUNCH(MFG_PROF_OTHER, b, 0.0, launch_sampler<double>(1, key[0], key[1], num, n, ld, (double *)out, s));
+  else
+    return MFG_ERR_BAD_ARG;
+  return MFG_OK;
+}
+
+int mfg_operator_apply(const mfg_operator *op, const void *V, void *W, int64_t p, int64_t ld,
+                       void *workspace, size_t workspace_bytes, void *stream) {
+  MFG_TRY(check_op(op));
+  MFG_TRY(check_panel(op, p, ld));
+  if (!V || !W || !aligned16(V) || !aligned16(W)) return MFG_ERR_BAD_ARG;
+  const WsLayout L = layout(op, 0, p, ld);
+  if (!workspace || workspace_bytes < L.total) return MFG_ERR_WORKSPACE;
+  char *ws = ws_base(workspace);
+  cudaStream_t s = as_stream(stream);
+  int *status = reinterpret_cast<int *>(ws + L.status);
+  if (op->precision == MFG_PREC_FP64)
+    return apply_op<double>(op, (const double *)V, ld, (double *)W, ld, p, nullptr, nullptr, ld,
+                            reinterpret_cast<double *>(ws + L.panel), status, s);
+  __nv_bfloat16 *hi = nullptr, *lo = nullptr;
+  if (uses_bf16(op)) {
+    hi = reinterpret_cast<__nv_bfloat16 *>(ws + L.hi);
+    lo = op->precision == MFG_PREC_BF16X3 ? reinterpret_cast<__nv_bfloat16 *>(ws + L.lo) : nullptr;
+    MFG_TRY(launch_split_bf16((const float *)V, p, op->n, ld, hi, lo, ld, s));
+  }
+  return apply_op<float>(op, (const float *)V, ld, (float *)W, ld, p, hi, lo, ld,
+                         reinterpret_cast<float *>(ws + L.panel), status, s);
+}
+
+int mfg_hessenberg(const mfg_operator *op, int64_t k, int64_t p, const void *V, int64_t ld,
+                   int32_t reortho, void *Q, double *H, void *residual, double *init_len_inv,
+                   void *workspace, size_t workspace_bytes, void *stream) {
+  MFG_TRY(check_op(op));
+  MFG_TRY(check_panel(op, p, ld));
+  if (k < 0 || k > op->n) return MFG_ERR_RANGE;
+  if (!V || !aligned16(V) || (k > 0 && (!Q || !H || !aligned16(Q)))) return MFG_ERR_BAD_ARG;
+  if (residual && !aligned16(residual)) return MFG_ERR_BAD_ARG;
+  if (reortho != 0 && reortho != 1) return MFG_ERR_BAD_ARG;
+  const WsLayout L = layout(op, k, p, ld);
+  if (!workspace || workspace_bytes < L.total) return MFG_ERR_WORKSPACE;
+  char *ws = ws_base(workspace);
+  cudaStream_t s = as_stream(stream);
+  if (op->precision == MFG_PREC_FP64)
+    return run_hessenberg<double>(op, k, p, (const double *)V, ld, reortho, (double *)Q, H,
+                                  (double *)residual, init_len_inv, L, ws, s);
+  return run_hessenberg<float>(op, k, p, (const float *)V, ld, reortho, (float *)Q, H,
+                               (float *)residual, init_len_inv, L, ws, s);
+}
+
+int mfg_tridiag_quadrature(int64_t k, int64_t p, const double *H, int32_t fun, double param,
+                           const double *scale, double *values, double *eigvals, double *first_sq,
+                           void *stream) {
+  if (k <= 0 || p <= 0 || !H || fun < MFG_FUN_LOG || fun > MFG_FUN_NONE) return MFG_ERR_BAD_ARG;
+  cudaStream_t s = as_stream(stream);
+  MFG_LAUNCH(MFG_PROF_QUAD, 8.0 * p * k * k + 16.0 * p * k, 0.0,
+             launch_tridiag_quadrature(k, p, H, fun, param, scale, values, eigvals, first_sq,
+                                       nullptr, s));
+  return MFG_OK;
+}
+
+int mfg_slq(const mfg_operator *op, int64_t k, int64_t p, const void *probes, int64_t ld,
+            int32_t fun, double param, double *values, double *mean_sem, void *Q, double *H,
+            void *workspace, size_t workspace_bytes, void *stream) {
+  MFG_TRY(check_op(op));
+  MFG_TRY(check_panel(op, p, ld));
+  if (k < 0 || k > op->n) return MFG_ERR_RANGE;
+  if (k == 0) return MFG_ERR_BAD_ARG;  // e1 of a 0 x 0 matrix does not exist
+  if (!probes || !aligned16(probes) || !values) return MFG_ERR_BAD_ARG;
+  if (fun < MFG_FUN_LOG || fun > MFG_FUN_POW) return MFG_ERR_BAD_ARG;
+  const WsLayout L = layout(op, k, p, ld);
+  if (!workspace || workspace_bytes < L.total) return MFG_ERR_WORKSPACE;
+  char *ws = ws_base(workspace);
+  cudaStream_t s = as_stream(stream);
+  void *Qb = Q ? Q : (void *)(ws + L.q);
+  double *Hb = H ? H : reinterpret_cast<double *>(ws + L.h);
+  double *len0 = reinterpret_cast<double *>(ws + L.len0);
+  double *scale = reinterpret_cast<double *>(ws + L.values);
+  int *status = reinterpret_cast<int *>(ws + L.status);
+  if (Q && !aligned16(Q)) return MFG_ERR_BAD_ARG;
+  if (op->precision == MFG_PREC_FP64)
+    MFG_TRY(run_hessenberg<double>(op, k, p, (const double *)probes, ld, 1, (double *)Qb, Hb,
+                                   nullptr, nullptr, L, ws, s));
+  else
+    MFG_TRY(run_hessenberg<float>(op, k, p, (const float *)probes, ld, 1, (float *)Qb, Hb, nullptr,
+                                  nullptr, L, ws, s));
+  // funm.py:240-241: length^2 * e1^T f(T) e1 with length = ||v||
+  MFG_LAUNCH(MFG_PROF_OTHER, 16.0 * p, (double)p, launch_square(len0, scale, p, s));
+  MFG_LAUNCH(MFG_PROF_QUAD, 8.0 * p * k * k + 16.0 * p * k, 0.0,
+             launch_tridiag_quadrature(k, p, Hb, fun, param, scale, values,
+                                       reinterpret_cast<double *>(ws + L.eig),
+                                       reinterpret_cast<double *>(ws + L.fsq), status, s));
+  if (mean_sem) MFG_LAUNCH(MFG_PROF_QUAD, 8.0 * p, 3.0 * p, launch_mean_sem(values, p, mean_sem, s));
+  return MFG_OK;
+}
+
+int mfg_rbf_build(const float *x, int64_t n, int32_t dim, double s2, double ell,
+                  int32_t precision, void *a, void *a_lo, int64_t lda, void *stream) {
+  if (!x || !a || n <= 0 || dim <= 0 || lda < n || lda % 8 != 0 || ell <= 0.0) return MFG_ERR_BAD_ARG;
+  if (precision == MFG_PREC_BF16X3 && !a_lo) return MFG_ERR_BAD_ARG;
+  if (precision < MFG_PREC_FP32 || precision > MFG_PREC_FP64) return MFG_ERR_BAD_ARG;
+  cudaStream_t s = as_stream(stream);
+  const double es = precision == MFG_PREC_FP64 ? 8.0 : (precision == MFG_PREC_FP32 ? 4.0 : (precision == MFG_PREC_BF16X3 ? 4.0 : 2.0));
+  MFG_LAUNCH(MFG_PROF_OTHER, (double)n * lda * es, 0.0,
+             launch_rbf_build(x, n, dim, s2, ell, precision, a, a_lo, lda, s));
+  return MFG_OK;
+}
+
+int mfg_split_bf16(const float *a, int64_t rows, int64_t cols, int64_t lda, void *hi, void *lo,
+                   int64_t ld_out, void *stream) {
+  if (!a || !hi || rows < 0 || cols < 0 || lda < cols || ld_out < cols) return MFG_ERR_BAD_ARG;
+  return launch_split_bf16(a, rows, cols, lda, (__nv_bfloat16 *)hi, (__nv_bfloat16 *)lo, ld_out,
+                           as_stream(stream));
+}
+
+}  // extern "C"

@@ -1,0 +1,75 @@
+// Shared helpers of the matfree_gb300 CUDA library (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+#include <stddef.h>
+
+#include "../../include/matfree_gb300.h"
+
+#define MFG_CUDA_TRY(expr)                                  \
+  do {                                                      \
+    cudaError_t _e = (expr);                                \
+    if (_e != cudaSuccess) return MFG_ERR_CUDA;             \
+  } while (0)
+
+#define MFG_TRY(expr)                                       \
+  do {                                                      \
+    int _s = (expr);                                        \
+    if (_s != MFG_OK) return _s;                            \
+  } while (0)
+
+namespace mfg {
+
+constexpr int kThreads = 256;  // threads per CTA of the streaming kernels
+constexpr int kWarps = kThreads / 32;
+
+inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// 16-byte vector type per element type: 4 floats or 2 doubles.
+template <typename T> struct Vec;
+template <> struct Vec<float> {
+  using type = float4;
+  static constexpr int width = 4;
+};
+template <> struct Vec<double> {
+  using type = double2;
+  static constexpr int width = 2;
+};
+
+template <typename T>
+__device__ __forceinline__ void vec_to_array(const typename Vec<T>::type &v, T *a);
+template <>
+__device__ __forceinline__ void vec_to_array<float>(const float4 &v, float *a) {
+  a[0] = v.x; a[1] = v.y; a[2] = v.z; a[3] = v.w;
+}
+template <>
+__device__ __forceinline__ void vec_to_array<double>(const double2 &v, double *a) {
+  a[0] = v.x; a[1] = v.y;
+}
+template <typename T>
+__device__ __forceinline__ typename Vec<T>::type array_to_vec(const T *a);
+template <>
+__device__ __forceinline__ float4 array_to_vec<float>(const float *a) {
+  return make_float4(a[0], a[1], a[2], a[3]);
+}
+template <>
+__device__ __forceinline__ double2 array_to_vec<double>(const double *a) {
+  return make_double2(a[0], a[1]);
+}
+
+// Accumulator type of the per-thread partial sums: float32 for float data
+// (combined in float64 across threads), float64 for double data.
+template <typename T> struct Acc { using type = T; };
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+}  // namespace mfg

@@ -1,0 +1,55 @@
+// Host-side launchers of the matfree_gb300 kernels (internal interface).
+#pragma once
+
+#include "common.cuh"
+
+namespace mfg {
+
+// lanczos_kernels.cu
+template <typename T>
+int launch_sampler(int stream_id, uint32_t k0, uint32_t k1, int64_t num, int64_t n, int64_t ld,
+                   T *out, cudaStream_t s);
+template <typename T> int64_t num_chunks(int64_t n);
+template <typename T>
+int launch_proj(const T *Q, int64_t q_bstride, int64_t q_istride, int ncols, const T *Wv,
+                int64_t w_bstride, int64_t n, int64_t p, double *partials, unsigned *counters,
+                double *out, int64_t out_bstride, int64_t out_istride, cudaStream_t s);
+template <typename T>
+int launch_sub(const T *Q, int64_t q_bstride, int64_t q_istride, int ncols, const double *coef,
+               int64_t c_bstride, int64_t c_istride, const T *Win, T *Wout, int64_t w_bstride,
+               int64_t n, int64_t p, bool with_norm, bool store, double *partials,
+               unsigned *counters, double *norm_out, double *norm_out2, int64_t norm2_bstride,
+               cudaStream_t s);
+template <typename T>
+int launch_scale(const T *Win, int64_t w_bstride, int64_t n, int64_t p, const double *norm, T *out,
+                 int64_t out_bstride, __nv_bfloat16 *hi, __nv_bfloat16 *lo, int64_t bf_bstride,
+                 cudaStream_t s);
+int launch_inv(const double *x, double *y, int64_t p, cudaStream_t s);
+
+// tridiag_quadrature.cu
+int launch_tridiag_quadrature(int64_t k, int64_t p, const double *H, int32_t fun, double param,
+                              const double *scale, double *values, double *eigvals,
+                              double *first_sq, int *status, cudaStream_t s);
+int launch_mean_sem(const double *values, int64_t p, double *mean_sem, cudaStream_t s);
+
+// operators.cu
+template <typename T>
+int launch_dense_simt(const T *A, int64_t lda, const T *V, int64_t ldv, T *W, int64_t ldw,
+                      int64_t n, int64_t p, double shift, cudaStream_t s);
+int launch_csr_spmm(const int32_t *row_ptr, const int32_t *col_idx, const float *val, int64_t n,
+                    const float *V, int64_t ldv, float *W, int64_t ldw, int64_t p, double shift,
+                    cudaStream_t s);
+int launch_rbf_build(const float *x, int64_t n, int dim, double s2, double ell, int precision,
+                     void *a, void *a_lo, int64_t lda, cudaStream_t s);
+int launch_split_bf16(const float *a, int64_t rows, int64_t cols, int64_t lda, __nv_bfloat16 *hi,
+                      __nv_bfloat16 *lo, int64_t ld_out, cudaStream_t s);
+
+// dense_tcgen05.cu: W = A V with A in bf16 (hi, optionally lo) and the panel
+// given as bf16 hi (and lo) copies; fp32 accumulate; W fp32 + shift * Vf.
+int launch_dense_tcgen05(const __nv_bfloat16 *A_hi, const __nv_bfloat16 *A_lo, int64_t lda,
+                         const __nv_bfloat16 *V_hi, const __nv_bfloat16 *V_lo, int64_t ldvb,
+                         const float *Vf, int64_t ldvf, float *W, int64_t ldw, int64_t n,
+                         int64_t p, double shift, int *status, cudaStream_t s);
+bool tcgen05_supported_shape(int64_t n, int64_t p);
+
+}  // namespace mfg

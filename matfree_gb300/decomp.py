@@ -1,0 +1,174 @@
+"""Krylov decompositions on the GPU: ``tridiag_sym`` and ``hessenberg``.
+
+Same constructors, call signature, outputs and errors as matfree/decomp.py:
+``tridiag_sym(num_matvecs, /, *, materialize=True, reortho="full",
+custom_vjp=True)`` returns ``decompose(matvec, vec, *params) ->
+_DecompResult(Q_tall, J_small, residual, init_length_inv)``
+(matfree/decomp.py:30-152).  As in matfree, the full-reorthogonalisation
+tridiagonalisation runs the Arnoldi iteration with classical Gram-Schmidt
+applied twice and returns the tridiagonal part of T = (H + H^T)/2
+(decomp.py:125-145).  The iteration itself runs in ``libmatfree_gb300``
+(``mfg_hessenberg``), batched over any number of vectors via ``.batched``.
+"""
+
+from __future__ import annotations
+
+import ctypes
+from typing import NamedTuple, Union
+
+import torch
+
+from . import _lib
+from ._panel import Workspace, as_panel, require_cuda, stream_ptr
+from .operators import as_operator
+from .tree import ravel_pytree
+
+
+class _DecompResult(NamedTuple):
+    # matfree/decomp.py:15-27
+    Q_tall: Union[torch.Tensor, tuple]
+    J_small: Union[torch.Tensor, tuple]
+    residual: torch.Tensor
+    init_length_inv: torch.Tensor
+
+
+def _error_num_matvecs(num, maxval, minval):
+    # matfree/decomp.py:753-756
+    msg1 = f"Parameter 'num_matvecs'={num} exceeds the acceptable range. "
+    msg2 = f"Expected: {minval} <= num_matvecs <= {maxval}."
+    return msg1 + msg2
+
+
+_WS = Workspace()
+
+
+def run_hessenberg(op, k: int, V: torch.Tensor, *, reortho: str = "full", workspace=None):
+    """Batched Arnoldi over the rows of V (p, n) on the GPU.
+
+    Returns (Q (p, k, n), H (p, k, k) float64, residual (p, n), 1/||v|| (p,)).
+    """
+    require_cuda(V, "vectors")
+    n = op.n
+    p = V.shape[0]
+    if k < 0 or k > n:
+        raise ValueError(_error_num_matvecs(k, maxval=n, minval=0))
+    dt = op.basis_dtype
+    panel, ld = as_panel(V, n, dt)
+    Q = torch.zeros((p, max(k, 0), ld), dtype=dt, device=V.device)
+    H = torch.zeros((p, k, k), dtype=torch.float64, device=V.device)
+    R = torch.zeros((p, ld), dtype=dt, device=V.device)
+    c = torch.zeros((p,), dtype=torch.float64, device=V.device)
+    s = op.c_struct()
+    lib = _lib.lib()
+    nbytes = lib.mfg_slq_workspace_bytes(ctypes.byref(s), k, p, ld)
+    ws, wsb = (workspace or _WS).get(nbytes, V.device)
+    st = lib.mfg_hessenberg(ctypes.byref(s), k, p, ctypes.c_void_p(panel.data_ptr()), ld,
+                            1 if reortho == "full" else 0,
+                            ctypes.c_void_p(Q.data_ptr() if k > 0 else 0),
+                            ctypes.c_void_p(H.data_ptr() if k > 0 else 0),
+                            ctypes.c_void_p(R.data_ptr()), ctypes.c_void_p(c.data_ptr()),
+                            ws, wsb, stream_ptr())
+    err = getattr(op, "error", None)
+    if err is not None:
+        op.error = None
+        raise err
+    _lib.check(st, "mfg_hessenberg")
+    return Q[:, :, :n], H, R[:, :n], c
+
+
+def _tridiag_from_hessenberg(H):
+    # matfree/decomp.py:133-135
+    T = 0.5 * (H + H.transpose(-1, -2))
+    return torch.diagonal(T, 0, -2, -1), torch.diagonal(T, 1, -2, -1)
+
+
+def _todense_tridiag_sym(diag, off_diag):
+    # matfree/decomp.py:148-152
+    return torch.diag_embed(diag) + torch.diag_embed(off_diag, -1) + torch.diag_embed(off_diag, 1)
+
+
+class _Decomposition:
+    reortho = "full"
+
+    def __init__(self, num_matvecs: int, *, materialize: bool, custom_vjp: bool):
+        self.num_matvecs = int(num_matvecs)
+        self.materialize = materialize
+        self.custom_vjp = custom_vjp
+
+    def _prepare(self, matvec, vec, params):
+        flat, unravel = ravel_pytree(vec)
+        n = flat.numel()
+        if self.num_matvecs < 0 or self.num_matvecs > n:
+            raise ValueError(_error_num_matvecs(self.num_matvecs, maxval=n, minval=0))
+        require_cuda(flat, "vec")
+        op = _flat_operator(matvec, unravel, n, flat.dtype, params)
+        return flat, unravel, op
+
+    def __call__(self, matvec, vec, *params):
+        flat, unravel, op = self._prepare(matvec, vec, params)
+        out = self.batched(op, flat[None, :])
+        Q, J, r, c = out
+        J = tuple(x[0] for x in J) if isinstance(J, tuple) else J[0]
+        return _DecompResult(Q_tall=unravel(Q[0]), J_small=J, residual=unravel(r[0]),
+                             init_length_inv=c[0])
+
+
+class _TridiagSymFull(_Decomposition):
+    def batched(self, matvec, V: torch.Tensor, *params) -> _DecompResult:
+        """Decompose every row of V (p, n) at once; outputs carry a leading p axis."""
+        op = as_operator(matvec, V.shape[1], V.dtype, params)
+        Q, H, r, c = run_hessenberg(op, self.num_matvecs, V, reortho="full")
+        d, e = _tridiag_from_hessenberg(H)
+        out_dt = V.dtype if V.dtype in (torch.float32, torch.float64) else torch.float32
+        d, e = d.to(out_dt), e.to(out_dt)
+        J = _todense_tridiag_sym(d, e) if self.materialize else (d, e)
+        return _DecompResult(Q_tall=Q, J_small=J, residual=r, init_length_inv=c.to(out_dt))
+
+
+class _Hessenberg(_Decomposition):
+    def __init__(self, num_matvecs, *, reortho, custom_vjp, reortho_vjp):
+        super().__init__(num_matvecs, materialize=True, custom_vjp=custom_vjp)
+        self.reortho = reortho
+        self.reortho_vjp = reortho if reortho_vjp == "match" else reortho_vjp
+
+    def batched(self, matvec, V: torch.Tensor, *params) -> _DecompResult:
+        op = as_operator(matvec, V.shape[1], V.dtype, params)
+        Q, H, r, c = run_hessenberg(op, self.num_matvecs, V, reortho=self.reortho)
+        out_dt = V.dtype if V.dtype in (torch.float32, torch.float64) else torch.float32
+        return _DecompResult(Q_tall=Q, J_small=H.to(out_dt), residual=r, init_length_inv=c.to(out_dt))
+
+
+def _flat_operator(matvec, unravel, n, dtype, params):
+    """The matvec over flat vectors (pytree in, pytree out, as decomp.py:383-384)."""
+    from .operators import CallbackOperator, Operator
+
+    if isinstance(matvec, Operator):
+        return as_operator(matvec, n, dtype, params)
+
+    def flat_fn(v, *p):
+        return ravel_pytree(matvec(unravel(v), *p))[0]
+
+    return CallbackOperator(flat_fn, n, dtype=dtype, params=params)
+
+
+def tridiag_sym(num_matvecs: int, /, *, materialize: bool = True, reortho: str = "full",
+                custom_vjp: bool = True):
+    """Tridiagonalisation with full reorthogonalisation (matfree/decomp.py:30-122)."""
+    if reortho == "full":
+        return _TridiagSymFull(num_matvecs, materialize=materialize, custom_vjp=custom_vjp)
+    if reortho == "none":
+        raise NotImplementedError(
+            "tridiag_sym(reortho='none') (three-term Lanczos without reorthogonalisation) is not "
+            "provided by matfree_gb300; use reortho='full'."
+        )
+    msg = f"reortho={reortho} unsupported. Choose eiter {'full', 'none'}."
+    raise ValueError(msg)
+
+
+def hessenberg(num_matvecs, /, *, reortho: str, custom_vjp: bool = True, reortho_vjp: str = "match"):
+    """Arnoldi / Hessenberg factorisation (matfree/decomp.py:353-423)."""
+    reortho_expected = ["none", "full"]
+    if reortho not in reortho_expected:
+        msg = f"Unexpected input for {reortho}: either of {reortho_expected} expected."
+        raise TypeError(msg)
+    return _Hessenberg(num_matvecs, reortho=reortho, custom_vjp=custom_vjp, reortho_vjp=reortho_vjp)

@@ -1,0 +1,189 @@
+"""Matrix functions and the SLQ integrands (GPU).
+
+``monte_carlo_funm_sym(dense_funm, tridiag_sym)`` and
+``monte_carlo_funm_sym_logdet(tridiag_sym)`` build the integrand
+``quadform(matvec, v, *params) = ||v||^2 e1^T f(T) e1`` of matfree/funm.py:186-243;
+``dense_funm_sym_eigh(matfun)`` is matfree/funm.py:322-335.  Called on one
+vector the integrand behaves exactly like matfree's.  The estimators in
+``stochtrace`` call ``integrand.batched(matvec, samples)`` instead of vmap:
+one ``mfg_slq`` call runs the Krylov iteration for all probes, then the
+batched tridiagonal eigensolve + quadrature kernel.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import math
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._panel import Workspace, as_panel, require_cuda, stream_ptr
+from .decomp import _flat_operator, _TridiagSymFull, run_hessenberg
+from .operators import Operator, as_operator
+from .tree import ravel_pytree
+
+_LOGS = {np.log, math.log, torch.log}
+_EXPS = {np.exp, math.exp, torch.exp}
+
+
+class DenseFunmSymEigh:
+    """f(M) = V diag(f(lambda)) V^T for a dense symmetric matrix (funm.py:322-335).
+
+    ``kind``/``param`` identify f for the fused device quadrature (log,
+    exp(param x), x**param); any other callable runs as torch code on the
+    eigenvalues produced by the device eigensolver.
+    """
+
+    def __init__(self, matfun, kind=None, param=0.0):
+        self.matfun = matfun
+        if kind is None:
+            if matfun in _LOGS:
+                kind, param = _lib.MFG_FUN_LOG, 0.0
+            elif matfun in _EXPS:
+                kind, param = _lib.MFG_FUN_EXP, 1.0
+        self.kind = kind
+        self.param = float(param)
+
+    def __call__(self, dense_matrix: torch.Tensor) -> torch.Tensor:
+        require_cuda(dense_matrix, "dense_matrix")
+        w, V = torch.linalg.eigh(dense_matrix)
+        return V @ torch.diag_embed(self.apply_scalar(w)) @ V.transpose(-1, -2)
+
+    def apply_scalar(self, x: torch.Tensor) -> torch.Tensor:
+        if self.kind == _lib.MFG_FUN_LOG:
+            return torch.log(x)
+        if self.kind == _lib.MFG_FUN_EXP:
+            return torch.exp(self.param * x)
+        if self.kind == _lib.MFG_FUN_POW:
+            return x ** self.param
+        out = self.matfun(x)
+        return out if isinstance(out, torch.Tensor) else torch.as_tensor(out, device=x.device)
+
+
+def dense_funm_sym_eigh(matfun):
+    """matfree/funm.py:322-335."""
+    return DenseFunmSymEigh(matfun)
+
+
+def funm_exp(scale: float = 1.0) -> DenseFunmSymEigh:
+    """f(x) = exp(scale x) with the fused device quadrature."""
+    return DenseFunmSymEigh(lambda x: torch.exp(scale * x), kind=_lib.MFG_FUN_EXP, param=scale)
+
+
+def funm_pow(power: float) -> DenseFunmSymEigh:
+    """f(x) = x ** power with the fused device quadrature."""
+    return DenseFunmSymEigh(lambda x: x ** power, kind=_lib.MFG_FUN_POW, param=power)
+
+
+_WS = Workspace()
+
+
+class MonteCarloFunmSym:
+    """The SLQ integrand (matfree/funm.py:205-243)."""
+
+    def __init__(self, dense_funm, tridiag_sym):
+        if not isinstance(dense_funm, DenseFunmSymEigh):
+            dense_funm = DenseFunmSymEigh(dense_funm)
+        if not isinstance(tridiag_sym, _TridiagSymFull):
+            raise TypeError("tridiag_sym must come from matfree_gb300.decomp.tridiag_sym(k, reortho='full')")
+        self.dense_funm = dense_funm
+        self.tridiag_sym = tridiag_sym
+
+    # single vector: the matfree call signature
+    def __call__(self, matvec, v0, *parameters):
+        flat, unravel = ravel_pytree(v0)
+        require_cuda(flat, "v0")
+        op = _flat_operator(matvec, unravel, flat.numel(), flat.dtype, parameters)
+        return self.batched(op, flat[None, :])[0]
+
+    def batched(self, matvec, samples: torch.Tensor, *parameters) -> torch.Tensor:
+        """Integrand values (p,) float64 for the rows of samples (p, n)."""
+        require_cuda(samples, "samples")
+        p, n = samples.shape
+        k = self.tridiag_sym.num_matvecs
+        if isinstance(matvec, Operator):
+            op = as_operator(matvec, n, samples.dtype, parameters)
+        else:
+            op = _flat_operator(matvec, lambda v: v, n, samples.dtype, parameters)
+        if k < 0 or k > n:
+            from .decomp import _error_num_matvecs
+
+            raise ValueError(_error_num_matvecs(k, maxval=n, minval=0))
+        if self.dense_funm.kind is not None:
+            return slq_values(op, k, samples, self.dense_funm.kind, self.dense_funm.param)
+        # arbitrary f: device Krylov + device eigensolve, f evaluated by torch on the GPU
+        _, H, _, c = run_hessenberg(op, k, samples, reortho="full")
+        lam, fsq = tridiag_eigh_first(H)
+        length_sq = 1.0 / (c * c)
+        return length_sq * (self.dense_funm.apply_scalar(lam) * fsq).sum(-1)
+
+
+def slq_values(op, k: int, samples: torch.Tensor, fun: int, param: float, mean_sem=None, workspace=None):
+    """One ``mfg_slq`` call: values (p,) float64 of ||v||^2 e1^T f(T) e1."""
+    p, n = samples.shape
+    panel, ld = as_panel(samples, n, op.basis_dtype)
+    values = torch.empty((p,), dtype=torch.float64, device=samples.device)
+    s = op.c_struct()
+    lib = _lib.lib()
+    nbytes = lib.mfg_slq_workspace_bytes(ctypes.byref(s), k, p, ld)
+    ws, wsb = (workspace or _WS).get(nbytes, samples.device)
+    ms = ctypes.c_void_p(mean_sem.data_ptr()) if mean_sem is not None else ctypes.c_void_p(0)
+    st = lib.mfg_slq(ctypes.byref(s), k, p, ctypes.c_void_p(panel.data_ptr()), ld, fun, param,
+                     ctypes.c_void_p(values.data_ptr()), ms, None, None, ws, wsb, stream_ptr())
+    err = getattr(op, "error", None)
+    if err is not None:
+        op.error = None
+        raise err
+    _lib.check(st, "mfg_slq")
+    return values
+
+
+def tridiag_eigh_first(H: torch.Tensor):
+    """Eigenvalues (ascending) and squared first eigenvector components of the
+    tridiagonal part of (H + H^T)/2 for a stack H (p, k, k) float64."""
+    p, k, _ = H.shape
+    H = H.contiguous()
+    lam = torch.empty((p, k), dtype=torch.float64, device=H.device)
+    fsq = torch.empty((p, k), dtype=torch.float64, device=H.device)
+    st = _lib.lib().mfg_tridiag_quadrature(k, p, ctypes.c_void_p(H.data_ptr()), _lib.MFG_FUN_NONE, 0.0,
+                                           None, None, ctypes.c_void_p(lam.data_ptr()),
+                                           ctypes.c_void_p(fsq.data_ptr()), stream_ptr())
+    _lib.check(st, "mfg_tridiag_quadrature")
+    return lam, fsq
+
+
+def monte_carlo_funm_sym(dense_funm, tridiag_sym, /):
+    """matfree/funm.py:205-243."""
+    return MonteCarloFunmSym(dense_funm, tridiag_sym)
+
+
+def monte_carlo_funm_sym_logdet(tridiag_sym, /):
+    """matfree/funm.py:186-202 (f = log)."""
+    return MonteCarloFunmSym(dense_funm_sym_eigh(torch.log), tridiag_sym)
+
+
+# The spec name of the same integrand.
+integrand_funm_sym_logdet = monte_carlo_funm_sym_logdet
+
+
+def funm_lanczos_sym(dense_funm, tridiag_sym, /):
+    """f(A) v via Lanczos (matfree/funm.py:114-147): ||v|| Q^T f(T) e1."""
+    if not isinstance(dense_funm, DenseFunmSymEigh):
+        dense_funm = DenseFunmSymEigh(dense_funm)
+
+    def estimate(matvec, vec, *parameters):
+        flat, unravel = ravel_pytree(vec)
+        require_cuda(flat, "vec")
+        length = torch.linalg.vector_norm(flat)
+        Q, T, *_ = tridiag_sym(_flat_operator(matvec, unravel, flat.numel(), flat.dtype, parameters)
+                               if not isinstance(matvec, Operator) else matvec, flat / length)
+        if isinstance(T, tuple):
+            from .decomp import _todense_tridiag_sym
+
+            T = _todense_tridiag_sym(*T)
+        fT = dense_funm(T.double())
+        return unravel(length * (Q.double().T @ fT[:, 0]).to(flat.dtype))
+
+    return estimate
