@@ -265,18 +265,20 @@ def roofline(prof, peaks, steps):
     """The class with the largest time share; HBM- or tensor-bound by its class."""
     total = sum(v["ms"] for v in prof.values()) or 1.0
     shares = {c: v["ms"] / total for c, v in prof.items()}
-    reortho_ms = prof["proj"]["ms"] + prof["sub"]["ms"]
-    reortho_b = prof["proj"]["bytes"] + prof["sub"]["bytes"]
+    cls = ("proj", "subproj", "sub")
+    reortho_ms = sum(prof[c]["ms"] for c in cls)
+    reortho_b = sum(prof[c]["bytes"] for c in cls)
     apply_ms = prof["apply"]["ms"]
-    launches_reortho = prof["proj"]["launches"] + prof["sub"]["launches"]
+    launches_reortho = sum(prof[c]["launches"] for c in cls)
     if reortho_ms >= apply_ms:
         per_launch_b = reortho_b / max(launches_reortho, 1)
         per_launch_s = reortho_ms / 1e3 / max(launches_reortho, 1)
         achieved = per_launch_b / per_launch_s / 1e9
-        return {"kernel": "cgs2 reortho (proj + sub)", "bound": "hbm", "achieved": achieved,
-                "peak": peaks["hbm"], "unit": "GB/s", "frac": achieved / peaks["hbm"],
-                "traffic": None, "time_share": (prof["proj"]["ms"] + prof["sub"]["ms"]) / total,
-                "launches": launches_reortho, "shares": shares}
+        return {"kernel": "cgs2 reortho sweeps (proj, subproj, sub)", "bound": "hbm",
+                "achieved": achieved, "peak": peaks["hbm"], "unit": "GB/s",
+                "frac": achieved / peaks["hbm"], "traffic": None, "time_share": reortho_ms / total,
+                "launches": launches_reortho, "shares": shares,
+                "per_class_gbs": {c: (prof[c]["bytes"] / (prof[c]["ms"] / 1e3) / 1e9 if prof[c]["ms"] else None) for c in cls}}
     fl = prof["apply"]["flops"]
     launches = max(prof["apply"]["launches"], 1)
     if fl > 0:

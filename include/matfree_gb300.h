@@ -41,7 +41,8 @@ enum {
   MFG_ERR_WORKSPACE = 3,   /* workspace smaller than mfg_slq_workspace_bytes  */
   MFG_ERR_CUDA = 4,        /* a CUDA runtime/driver call failed               */
   MFG_ERR_UNSUPPORTED = 5, /* combination not implemented (e.g. op/precision) */
-  MFG_ERR_NO_CONVERGENCE = 6 /* tridiagonal eigensolver hit its sweep limit   */
+  MFG_ERR_NO_CONVERGENCE = 6, /* tridiagonal eigensolver hit its sweep limit  */
+  MFG_ERR_TIMEOUT = 7      /* a bounded device-side wait gave up             */
 };
 
 /* ---- element type of vectors and bases --------------------------------- */
@@ -166,7 +167,8 @@ enum {
   MFG_PROF_SCALE = 3,  /* normalisation (+ bf16 split of the new vector)        */
   MFG_PROF_QUAD = 4,   /* tridiagonal eigensolve + quadrature + mean            */
   MFG_PROF_OTHER = 5,  /* samplers, operator builds, initial norms              */
-  MFG_PROF_CLASSES = 6
+  MFG_PROF_SUBPROJ = 6, /* fused update + second projection (one basis read)   */
+  MFG_PROF_CLASSES = 7
 };
 
 /* Reset the process-wide launch counters; timing != 0 also brackets every

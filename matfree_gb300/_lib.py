@@ -19,6 +19,7 @@ MFG_ERR_WORKSPACE = 3
 MFG_ERR_CUDA = 4
 MFG_ERR_UNSUPPORTED = 5
 MFG_ERR_NO_CONVERGENCE = 6
+MFG_ERR_TIMEOUT = 7
 
 MFG_F32, MFG_F64 = 0, 1
 MFG_OP_DENSE, MFG_OP_CSR, MFG_OP_CALLBACK = 0, 1, 2
@@ -65,7 +66,7 @@ SIGNATURES = {
     "mfg_profile_read": (c_int, [c_int32, POINTER(c_double), POINTER(c_double), POINTER(c_double), POINTER(c_int64)]),
 }
 
-PROF_CLASSES = ["apply", "proj", "sub", "scale", "quad", "other"]
+PROF_CLASSES = ["apply", "proj", "sub", "scale", "quad", "other", "subproj"]
 
 _LIB = None
 

@@ -92,7 +92,8 @@ static bool uses_bf16(const mfg_operator *op) {
 static WsLayout layout(const mfg_operator *op, int64_t k, int64_t p, int64_t ld) {
   WsLayout L{};
   const size_t es = (size_t)elem_size_for(op);
-  const int64_t nch = es == 8 ? num_chunks<double>(op->n) : num_chunks<float>(op->n);
+  // the fused update+projection uses the smallest chunks (256 rows)
+  const int64_t nch = es == 8 ? max_fused_chunks<double>(op->n) : max_fused_chunks<float>(op->n);
   const int64_t kk = k > 0 ? k : 1;
   size_t off = 0;
   auto take = [&](size_t bytes) {
@@ -264,7 +265,15 @@ static int run_hessenberg(const mfg_operator *op, int64_t k, int64_t p, const T 
                launch_proj<T>(Q, qb, ld, ncols, Wb, ld, n, p, partials, counters, H + j, k * k, k, s));
     const bool last = (j + 1 == k);
     double *hsub = last ? nullptr : H + (j + 1) * k + j;
-    if (reortho) {
+    if (reortho && sub_proj_rows_per_thread<T>(ncols) > 0) {
+      // w' = w - Q h1 and h2 = Q^T w' from one read of the basis
+      MFG_LAUNCH(MFG_PROF_SUBPROJ, (ncols + 2.0) * vecb, 2.0 * pf,
+                 launch_sub_proj<T>(Q, qb, ld, ncols, H + j, k * k, k, Wb, ld, n, p, partials,
+                                    counters, h2, k, status, s));
+      MFG_LAUNCH(MFG_PROF_SUB, ub, pf + 2.0 * vecb / sizeof(T),
+                 launch_sub<T>(Q, qb, ld, ncols, h2, k, 1, Wb, Wb, ld, n, p, true, true, partials,
+                               counters, norm, hsub, k * k, s));
+    } else if (reortho) {
       MFG_LAUNCH(MFG_PROF_SUB, ub, pf,
                  launch_sub<T>(Q, qb, ld, ncols, H + j, k * k, k, Wb, Wb, ld, n, p, false, true,
                                partials, counters, norm, nullptr, 0, s));
@@ -347,6 +356,7 @@ const char *mfg_status_string(int status) {
     case MFG_ERR_CUDA: return "CUDA error";
     case MFG_ERR_UNSUPPORTED: return "unsupported operator/precision/shape";
     case MFG_ERR_NO_CONVERGENCE: return "tridiagonal eigensolver did not converge";
+    case MFG_ERR_TIMEOUT: return "a bounded device-side wait timed out";
     default: return "unknown status";
   }
 }

@@ -1,17 +1,387 @@
-// Dense W = A V on the 5th-generation tensor cores (placeholder until the
-// tcgen05 kernel lands; the bf16 precisions report MFG_ERR_UNSUPPORTED).
+// Dense operator application W = A V on the 5th-generation tensor cores.
+//
+//   W[b][m] = sum_k A[m][k] V[b][k] + shift * Vf[b][m]
+//
+// A (n x n, row-major, bf16 hi and optionally lo) and the probe panel V
+// (p rows of bf16, hi and optionally lo) are both K-major, so one tile of the
+// product is the UMMA D[M = 128 rows of A][N = probes] += A_tile[M][K] B[N][K]^T.
+//
+// CTA organisation (192 threads, one output tile of 128 rows x BN probes):
+//   warp 0      TMA producer: one elected lane streams 32-wide K slices of A
+//               (and A_lo) and of the panel (and its lo part) into a ring of
+//               shared-memory stages (64-byte swizzled rows, 1024-byte aligned
+//               tiles; 4 stages in split mode, 8 in plain bf16) and arms the
+//               stage's "full" mbarrier with the transaction bytes.
+//   warp 1      allocates the TMEM accumulator (BN fp32 columns x 128 lanes);
+//               one lane issues tcgen05.mma (kind::f16, bf16 inputs, fp32
+//               accumulate), 2 per K slice (K = 16 each), 6 for the split
+//               product hi*hi + hi*lo + lo*hi, then tcgen05.commit to the
+//               stage's "empty" mbarrier; a final commit signals the epilogue.
+//   warps 2-5   epilogue: tcgen05.ld 32 lanes x 16 columns at a time (each
+//               warp owns the TMEM lane quarter its warp index allows), add
+//               shift * Vf and store; 32 lanes write 32 consecutive rows of
+//               one probe (128-byte coalesced stores).
+//
+// Every mbarrier wait is bounded.  A role that gives up records
+// MFG_ERR_TIMEOUT in *status and raises a shared abort flag; the others leave
+// their loops, in-flight TMA copies and MMAs are drained with bounded waits,
+// and the TMEM columns are freed before the CTA exits.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <mutex>
+
 #include "common.cuh"
 #include "kernels.cuh"
 
 namespace mfg {
 
-bool tcgen05_supported_shape(int64_t, int64_t) { return false; }
+constexpr int kBM = 128;            // rows of A per tile (UMMA M)
+constexpr int kBK = 32;             // K per stage: one swizzle atom row of bf16
+constexpr int kRowBytes = kBK * 2;  // 64-byte rows -> SWIZZLE_64B (128 -> SWIZZLE_128B)
+static_assert(kRowBytes == 64 || kRowBytes == 128, "supported swizzle widths");
+constexpr int kUmmaK = 16;          // K per tcgen05.mma of kind::f16
+constexpr int kGemmThreads = 192;
+constexpr uint32_t kWaitLimit = 1u << 24;  // bounded spin on every mbarrier
 
-int launch_dense_tcgen05(const __nv_bfloat16 *, const __nv_bfloat16 *, int64_t,
-                         const __nv_bfloat16 *, const __nv_bfloat16 *, int64_t, const float *,
-                         int64_t, float *, int64_t, int64_t, int64_t, double, int *,
-                         cudaStream_t) {
-  return MFG_ERR_UNSUPPORTED;
+struct GemmShared {
+  uint64_t full[8];
+  uint64_t empty[8];
+  uint64_t tmem_full;
+  uint64_t drain;
+  uint32_t tmem_base;
+  int abort;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait; gives up early when another role raised the abort flag.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort_flag,
+                                          int *status) {
+  for (uint32_t it = 0; it < kWaitLimit; ++it) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((it & 1023u) == 1023u && *abort_flag) return false;
+  }
+  *abort_flag = 1;
+  if (status) atomicExch(status, (int)MFG_ERR_TIMEOUT);
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, uint64_t *bar, int x,
+                                            int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];"
+      ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(x), "r"(y)
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+// UMMA shared-memory descriptor of a K-major swizzled tile whose rows are
+// kRowBytes apart (the TMA box width): stride between 8-row groups (SBO) =
+// 8 * kRowBytes, descriptor version 1, layout type 4 (SWIZZLE_64B) or 2
+// (SWIZZLE_128B).  The leading-byte offset is not used by swizzled K-major
+// layouts and is set to 1.
+__device__ __forceinline__ uint64_t sw_desc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)1u << 16;
+  d |= (uint64_t)((8u * kRowBytes) >> 4) << 32;
+  d |= (uint64_t)1u << 46;
+  d |= (uint64_t)(kRowBytes == 128 ? 2u : 4u) << 61;
+  return d;
+}
+
+// Instruction descriptor of kind::f16: D fp32, A and B bf16, both K-major.
+__host__ __device__ constexpr uint32_t instr_desc_bf16(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
+                                          uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n"
+      ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t *bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                   smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+template <bool kSplit>
+__global__ void __launch_bounds__(kGemmThreads, 1)
+dense_tcgen05_kernel(const __grid_constant__ CUtensorMap map_ahi,
+                     const __grid_constant__ CUtensorMap map_alo,
+                     const __grid_constant__ CUtensorMap map_bhi,
+                     const __grid_constant__ CUtensorMap map_blo, const float *__restrict__ Vf,
+                     int64_t ldvf, float *__restrict__ W, int64_t ldw, int n, int p, int BN,
+                     int stages, uint32_t tmem_cols, float shift, int *status) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  // 1024-byte aligned stage ring, then the barrier block
+  uint8_t *tiles = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+  const uint32_t a_bytes = kBM * kBK * 2;
+  const uint32_t b_bytes = (uint32_t)BN * kBK * 2;
+  const uint32_t stage_bytes = (kSplit ? 2u : 1u) * (a_bytes + b_bytes);
+  GemmShared *sh = reinterpret_cast<GemmShared *>(tiles + (size_t)stages * stage_bytes);
+
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const int m0 = blockIdx.x * kBM;
+  const int b0 = blockIdx.y * BN;
+  const int num_k = (n + kBK - 1) / kBK;
+  volatile int *abort_flag = &sh->abort;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < stages; ++s) {
+      mbar_init(&sh->full[s], 1);
+      mbar_init(&sh->empty[s], 1);
+    }
+    mbar_init(&sh->tmem_full, 1);
+    mbar_init(&sh->drain, 1);
+    sh->abort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&sh->tmem_base)),
+                 "r"(tmem_cols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = sh->tmem_base;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      int issued = 0;
+      for (int kt = 0; kt < num_k; ++kt) {
+        const int s = kt % stages;
+        const uint32_t ph = (uint32_t)(kt / stages) & 1u;
+        if (!mbar_wait(&sh->empty[s], ph ^ 1u, abort_flag, status)) break;
+        uint8_t *st = tiles + (size_t)s * stage_bytes;
+        mbar_arrive_expect_tx(&sh->full[s], stage_bytes);
+        const int kx = kt * kBK;
+        tma_load_2d(st, &map_ahi, &sh->full[s], kx, m0);
+        tma_load_2d(st + a_bytes, &map_bhi, &sh->full[s], kx, b0);
+        if (kSplit) {
+          tma_load_2d(st + a_bytes + b_bytes, &map_alo, &sh->full[s], kx, m0);
+          tma_load_2d(st + 2 * a_bytes + b_bytes, &map_blo, &sh->full[s], kx, b0);
+        }
+        ++issued;
+      }
+      // drain: copies still in flight complete their stage's "full" phase
+      if (*abort_flag) {
+        for (int kt = (issued > stages ? issued - stages : 0); kt < issued; ++kt) {
+          const int s = kt % stages;
+          const uint32_t ph = (uint32_t)(kt / stages) & 1u;
+          for (uint32_t it = 0; it < kWaitLimit && !mbar_try_wait(&sh->full[s], ph); ++it) {
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      const uint32_t idesc = instr_desc_bf16(kBM, BN);
+      int done = 0;
+      for (int kt = 0; kt < num_k; ++kt) {
+        const int s = kt % stages;
+        const uint32_t ph = (uint32_t)(kt / stages) & 1u;
+        if (!mbar_wait(&sh->full[s], ph, abort_flag, status)) break;
+        tc_fence_after();
+        const uint32_t st = smem_u32(tiles + (size_t)s * stage_bytes);
+        const uint32_t ahi = st, bhi = st + a_bytes;
+        const uint32_t alo = st + a_bytes + b_bytes, blo = st + 2 * a_bytes + b_bytes;
+#pragma unroll
+        for (int kk = 0; kk < kBK / kUmmaK; ++kk) {
+          const uint32_t off = (uint32_t)kk * kUmmaK * 2;  // 32 bytes along K inside the atom
+          const uint32_t acc = (kt > 0 || kk > 0) ? 1u : 0u;
+          umma_bf16(tmem, sw_desc(ahi + off), sw_desc(bhi + off), idesc, acc);
+          if (kSplit) {
+            umma_bf16(tmem, sw_desc(ahi + off), sw_desc(blo + off), idesc, 1u);
+            umma_bf16(tmem, sw_desc(alo + off), sw_desc(bhi + off), idesc, 1u);
+          }
+        }
+        umma_commit(&sh->empty[s]);
+        ++done;
+      }
+      // every MMA issued so far completes before this arrives
+      umma_commit(done == num_k ? &sh->tmem_full : &sh->drain);
+      if (done != num_k) {
+        for (uint32_t it = 0; it < kWaitLimit && !mbar_try_wait(&sh->drain, 0); ++it) {
+        }
+      }
+    }
+  } else {
+    // epilogue: warps 2..5 -> TMEM lane quarters 2, 3, 0, 1
+    const int quarter = warp & 3;
+    const int row = quarter * 32 + lane;
+    const int m = m0 + row;
+    // warp-uniform decision: tcgen05.ld is executed by all 32 lanes or none
+    const bool ok = __all_sync(0xffffffffu, mbar_wait(&sh->tmem_full, 0, abort_flag, status));
+    tc_fence_after();
+    if (ok) {
+      for (int c = 0; c < BN; c += 16) {
+        float v[16];
+        tmem_ld16(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)c, v);
+        if (m < n) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int b = b0 + c + j;
+            if (b < p) {
+              float out = v[j];
+              if (shift != 0.f) out = fmaf(shift, __ldg(Vf + (int64_t)b * ldvf + m), out);
+              W[(int64_t)b * ldw + m] = out;
+            }
+          }
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(tmem_cols)
+                 : "memory");
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *ptr = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(ptr);
+  });
+  return fn;
+}
+
+// 2-D bf16 map: inner extent `cols` (K), `rows` rows `ld` elements apart,
+// box 64 x box_rows, 128-byte swizzle, zero fill out of bounds.
+static bool make_map(CUtensorMap *map, const void *base, int64_t cols, int64_t rows, int64_t ld,
+                     uint32_t box_rows) {
+  auto fn = encode_fn();
+  if (!fn) return false;
+  cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+  cuuint32_t box[2] = {(cuuint32_t)kBK, box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides, box,
+            estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            kRowBytes == 128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+bool tcgen05_supported_shape(int64_t n, int64_t p) {
+  return n > 0 && p > 0 && n < (1ll << 31) && p < (1ll << 31) && encode_fn() != nullptr;
+}
+
+int launch_dense_tcgen05(const __nv_bfloat16 *A_hi, const __nv_bfloat16 *A_lo, int64_t lda,
+                         const __nv_bfloat16 *V_hi, const __nv_bfloat16 *V_lo, int64_t ldvb,
+                         const float *Vf, int64_t ldvf, float *W, int64_t ldw, int64_t n, int64_t p,
+                         double shift, int *status, cudaStream_t s) {
+  if (n <= 0 || p <= 0) return MFG_OK;
+  if (!tcgen05_supported_shape(n, p)) return MFG_ERR_UNSUPPORTED;
+  const bool split = (A_lo != nullptr);
+  if (split && V_lo == nullptr) return MFG_ERR_BAD_ARG;
+  if (lda % 8 != 0 || ldvb % 8 != 0 || ((uintptr_t)A_hi & 15) || ((uintptr_t)V_hi & 15))
+    return MFG_ERR_BAD_ARG;
+  // probes per tile: a multiple of 16 in [16, 256]
+  const int64_t pt = p < 256 ? p : 256;
+  const int BN = (int)((pt + 15) / 16 * 16);
+  uint32_t cols = 32;
+  while ((int)cols < BN) cols <<= 1;
+  const uint32_t a_bytes = kBM * kBK * 2, b_bytes = (uint32_t)BN * kBK * 2;
+  const uint32_t stage_bytes = (split ? 2u : 1u) * (a_bytes + b_bytes);
+  const size_t budget = 200 * 1024;
+  int stages = (int)(budget / stage_bytes);
+  if (stages > 8) stages = 8;
+  if (stages < 2) return MFG_ERR_UNSUPPORTED;
+  const size_t smem = 1024 + (size_t)stages * stage_bytes + sizeof(GemmShared);
+
+  CUtensorMap mahi, malo, mbhi, mblo;
+  if (!make_map(&mahi, A_hi, n, n, lda, kBM)) return MFG_ERR_CUDA;
+  if (!make_map(&mbhi, V_hi, n, p, ldvb, (uint32_t)BN)) return MFG_ERR_CUDA;
+  if (split) {
+    if (!make_map(&malo, A_lo, n, n, lda, kBM)) return MFG_ERR_CUDA;
+    if (!make_map(&mblo, V_lo, n, p, ldvb, (uint32_t)BN)) return MFG_ERR_CUDA;
+  } else {
+    malo = mahi;
+    mblo = mbhi;
+  }
+  dim3 grid((unsigned)((n + kBM - 1) / kBM), (unsigned)((p + BN - 1) / BN));
+  if (grid.y > 65535) return MFG_ERR_UNSUPPORTED;
+  if (split) {
+    MFG_CUDA_TRY(cudaFuncSetAttribute(dense_tcgen05_kernel<true>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dense_tcgen05_kernel<true><<<grid, kGemmThreads, smem, s>>>(
+        mahi, malo, mbhi, mblo, Vf, ldvf, W, ldw, (int)n, (int)p, BN, stages, cols, (float)shift,
+        status);
+  } else {
+    MFG_CUDA_TRY(cudaFuncSetAttribute(dense_tcgen05_kernel<false>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dense_tcgen05_kernel<false><<<grid, kGemmThreads, smem, s>>>(
+        mahi, malo, mbhi, mblo, Vf, ldvf, W, ldw, (int)n, (int)p, BN, stages, cols, (float)shift,
+        status);
+  }
+  return cudaGetLastError() == cudaSuccess ? MFG_OK : MFG_ERR_CUDA;
 }
 
 }  // namespace mfg

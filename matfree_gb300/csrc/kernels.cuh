@@ -20,6 +20,13 @@ int launch_sub(const T *Q, int64_t q_bstride, int64_t q_istride, int ncols, cons
                int64_t n, int64_t p, bool with_norm, bool store, double *partials,
                unsigned *counters, double *norm_out, double *norm_out2, int64_t norm2_bstride,
                cudaStream_t s);
+template <typename T> int sub_proj_rows_per_thread(int ncols);
+template <typename T> int64_t max_fused_chunks(int64_t n);
+template <typename T>
+int launch_sub_proj(const T *Q, int64_t q_bstride, int64_t q_istride, int ncols, const double *coef,
+                    int64_t c_bstride, int64_t c_istride, T *Wv, int64_t w_bstride, int64_t n,
+                    int64_t p, double *partials, unsigned *counters, double *out,
+                    int64_t out_bstride, int *status, cudaStream_t s);
 template <typename T>
 int launch_scale(const T *Win, int64_t w_bstride, int64_t n, int64_t p, const double *norm, T *out,
                  int64_t out_bstride, __nv_bfloat16 *hi, __nv_bfloat16 *lo, int64_t bf_bstride,

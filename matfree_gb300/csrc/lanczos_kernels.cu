@@ -154,7 +154,46 @@ __device__ __forceinline__ bool arrive_last(unsigned *counters, int64_t b, int n
 // ---------------------------------------------------------------------------
 
 constexpr int kColGroup = 8;  // columns reduced together (independent loads in flight)
+constexpr int kMaxProjCols = 768;  // ncols * kWarps doubles of shared memory <= 48 KB
 
+// Warp tree in the data type: one warp partial sums 32 lanes' products.
+template <typename T>
+__device__ __forceinline__ T warp_sum_t(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Sum the nred per-warp partials red[i][0..nred) of this CTA (float64) and
+// finish the cross-CTA reduction of column i for probe b.
+__device__ __forceinline__ void finish_columns(const double *red, int ncols, int64_t b, int64_t c,
+                                               int nchunks, double *partials, unsigned *counters,
+                                               double *out, int64_t out_bstride,
+                                               int64_t out_istride, int nred = kWarps) {
+  for (int i = threadIdx.x; i < ncols; i += kThreads) {
+    double t = 0.0;
+    for (int q = 0; q < nred; ++q) t += red[i * nred + q];
+    if (nchunks == 1)
+      out[b * out_bstride + i * out_istride] = t;
+    else
+      partials[(b * nchunks + c) * ncols + i] = t;
+  }
+  if (nchunks == 1) return;
+  if (arrive_last(counters, b, nchunks)) {
+    for (int i = threadIdx.x; i < ncols; i += kThreads) {
+      double t = 0.0;
+      for (int cc = 0; cc < nchunks; ++cc) t += __ldcg(&partials[(b * nchunks + cc) * ncols + i]);
+      out[b * out_bstride + i * out_istride] = t;
+    }
+    if (threadIdx.x == 0) counters[b] = 0u;
+  }
+}
+
+// h = Q^T w for the first ncols basis vectors.  Each thread forms kVPT*width
+// products per column in the data type, a warp sums its 32 lanes in the data
+// type (256 products), and warps, chunks and the final value are combined in
+// float64.  Warps run through the columns without block barriers; their
+// partials meet in shared memory once at the end.
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
 proj_kernel(const T *__restrict__ Q, int64_t q_bstride, int64_t q_istride, int ncols,
@@ -162,7 +201,7 @@ proj_kernel(const T *__restrict__ Q, int64_t q_bstride, int64_t q_istride, int n
             double *__restrict__ partials, unsigned *__restrict__ counters,
             double *__restrict__ out, int64_t out_bstride, int64_t out_istride) {
   constexpr int W = Vec<T>::width;
-  __shared__ double red[kColGroup][kWarps];
+  extern __shared__ double red[];  // [ncols][kWarps]
   const int64_t c = blockIdx.x;
   const int64_t b = blockIdx.y;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -171,7 +210,7 @@ proj_kernel(const T *__restrict__ Q, int64_t q_bstride, int64_t q_istride, int n
   load_chunk<T>(Wv + b * w_bstride, n, c, w);
 
   for (int i0 = 0; i0 < ncols; i0 += kColGroup) {
-    double s[kColGroup];
+    T s[kColGroup];
 #pragma unroll
     for (int g = 0; g < kColGroup; ++g) {
       T acc = (T)0;
@@ -183,36 +222,158 @@ proj_kernel(const T *__restrict__ Q, int64_t q_bstride, int64_t q_istride, int n
 #pragma unroll
           for (int u = 0; u < W; ++u) acc = fma(q[e][u], w[e][u], acc);
       }
-      s[g] = (double)acc;
+      s[g] = acc;
     }
 #pragma unroll
-    for (int g = 0; g < kColGroup; ++g) s[g] = warp_sum(s[g]);
+    for (int g = 0; g < kColGroup; ++g) s[g] = warp_sum_t<T>(s[g]);
     if (lane == 0) {
 #pragma unroll
-      for (int g = 0; g < kColGroup; ++g) red[g][warp] = s[g];
+      for (int g = 0; g < kColGroup; ++g)
+        if (i0 + g < ncols) red[(i0 + g) * kWarps + warp] = (double)s[g];
     }
-    __syncthreads();
-    if (threadIdx.x < kColGroup && i0 + (int)threadIdx.x < ncols) {
-      double t = 0.0;
+  }
+  __syncthreads();
+  finish_columns(red, ncols, b, c, nchunks, partials, counters, out, out_bstride, out_istride);
+}
+
+// ---------------------------------------------------------------------------
+// Fused second pass: w' = w - Q c, then h2 = Q^T w' from one read of Q.
+//
+// The CTA owns R = kThreads * EPT consecutive rows of one probe.  One thread
+// issues a bulk asynchronous copy per basis vector (its R-row segment) into
+// shared memory, all completing on one mbarrier; the CTA then forms w' from
+// shared memory, stores it, and reads the same shared tile again for the
+// projections.  This removes one of the four basis sweeps of a CGS2 step.
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+constexpr uint32_t kBarWaitLimit = 1u << 24;
+constexpr int kSPGroup = 8;                                    // columns per copy barrier
+constexpr int kMaxSPGroups = (kMaxProjCols + kSPGroup - 1) / kSPGroup;
+constexpr size_t kSubProjSmemBudget = 110 * 1024;              // two CTAs per SM
+
+__device__ __forceinline__ bool bar_try_wait0(uint64_t *bar) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(ok)
+      : "r"(smem_addr(bar))
+      : "memory");
+  return ok != 0;
+}
+
+template <typename T, int EPT>
+__global__ void __launch_bounds__(kThreads)
+sub_proj_kernel(const T *__restrict__ Q, int64_t q_bstride, int64_t q_istride, int ncols,
+                const double *__restrict__ coef, int64_t c_bstride, int64_t c_istride,
+                T *Wv, int64_t w_bstride, int64_t n, int nchunks, double *__restrict__ partials,
+                unsigned *__restrict__ counters, double *__restrict__ out, int64_t out_bstride,
+                int *__restrict__ status) {
+  constexpr int R = kThreads * EPT;
+  extern __shared__ __align__(128) uint8_t smem[];
+  T *qs = reinterpret_cast<T *>(smem);                       // [ncols][R]
+  T *ws = qs + (size_t)ncols * R;                            // [R]  w' of this chunk
+  T *s_coef = ws + R;                                        // [ncols]
+  double *red = reinterpret_cast<double *>(s_coef + ((ncols + 1) & ~1));  // [ncols]
+  __shared__ __align__(8) uint64_t bars[kMaxSPGroups];
+  __shared__ int s_fail;
+
+  const int64_t c = blockIdx.x;
+  const int64_t b = blockIdx.y;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t r0 = c * R;
+  const int64_t rows = (n - r0 < R) ? (n - r0) : R;
+  const uint32_t seg_bytes = (uint32_t)(((rows * (int64_t)sizeof(T)) + 15) / 16 * 16);
+  const int ngroups = (ncols + kSPGroup - 1) / kSPGroup;
+
+  if (threadIdx.x == 0) {
+    for (int g = 0; g < ngroups; ++g)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bars[g])) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    s_fail = 0;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    // one barrier per group of columns: the update consumes columns as they
+    // land.  Lane 0 arms every barrier; the 32 lanes issue the copies.
+    if (lane == 0) {
+      for (int g = 0; g < ngroups; ++g) {
+        const int i1 = (g + 1) * kSPGroup < ncols ? (g + 1) * kSPGroup : ncols;
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
+                         smem_addr(&bars[g])),
+                     "r"(seg_bytes * (uint32_t)(i1 - g * kSPGroup))
+                     : "memory");
+      }
+    }
+    for (int i = lane; i < ncols; i += 32) {
+      const T *src = Q + b * q_bstride + (int64_t)i * q_istride + r0;
+      asm volatile(
+          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+          ::"r"(smem_addr(qs + (size_t)i * R)), "l"(reinterpret_cast<uint64_t>(src)),
+          "r"(seg_bytes), "r"(smem_addr(&bars[i / kSPGroup]))
+          : "memory");
+    }
+  }
+  for (int i = threadIdx.x; i < ncols; i += kThreads) s_coef[i] = (T)coef[b * c_bstride + i * c_istride];
+
+  // this thread's EPT consecutive rows
+  const int64_t rt = r0 + (int64_t)threadIdx.x * EPT;
+  T w[EPT];
 #pragma unroll
-      for (int q = 0; q < kWarps; ++q) t += red[threadIdx.x][q];
-      const int i = i0 + threadIdx.x;
-      if (nchunks == 1)
-        out[b * out_bstride + i * out_istride] = t;
-      else
-        partials[(b * nchunks + c) * ncols + i] = t;
+  for (int e = 0; e < EPT; ++e) w[e] = (rt + e < n) ? Wv[b * w_bstride + rt + e] : (T)0;
+  __syncthreads();
+
+  const T *qrow = qs + (size_t)threadIdx.x * EPT;
+  volatile int *fail = &s_fail;
+  for (int g = 0; g < ngroups; ++g) {
+    // bounded wait for this group's basis segments
+    bool ready = false;
+    for (uint32_t it = 0; it < kBarWaitLimit; ++it) {
+      if (bar_try_wait0(&bars[g])) {
+        ready = true;
+        break;
+      }
+      if ((it & 1023u) == 1023u && *fail) break;
     }
-    __syncthreads();
-  }
-  if (nchunks == 1) return;
-  if (arrive_last(counters, b, nchunks)) {
-    for (int i = threadIdx.x; i < ncols; i += kThreads) {
-      double t = 0.0;
-      for (int cc = 0; cc < nchunks; ++cc) t += __ldcg(&partials[(b * nchunks + cc) * ncols + i]);
-      out[b * out_bstride + i * out_istride] = t;
+    if (!ready) {
+      *fail = 1;
+      if (status) atomicExch(status, (int)MFG_ERR_TIMEOUT);
+      break;
     }
-    if (threadIdx.x == 0) counters[b] = 0u;
+    const int i1 = (g + 1) * kSPGroup < ncols ? (g + 1) * kSPGroup : ncols;
+    for (int i = g * kSPGroup; i < i1; ++i) {
+      const T ci = s_coef[i];
+#pragma unroll
+      for (int e = 0; e < EPT; ++e) w[e] = fma(-qrow[(size_t)i * R + e], ci, w[e]);
+    }
   }
+  __syncthreads();
+  if (s_fail) return;
+#pragma unroll
+  for (int e = 0; e < EPT; ++e) {
+    if (rt + e < n) Wv[b * w_bstride + rt + e] = w[e];
+    ws[threadIdx.x * EPT + e] = (rt + e < n) ? w[e] : (T)0;
+  }
+  __syncthreads();
+
+  // h2: warp `warp` owns columns warp, warp + 8, ...; its lanes stride the
+  // R rows of the chunk, so one warp reduction covers R products.  Rows past
+  // n hold stale shared memory and are left out.
+  for (int i = warp; i < ncols; i += kWarps) {
+    const T *col = qs + (size_t)i * R;
+    T acc = (T)0;
+#pragma unroll 4
+    for (int r = lane; r < R; r += 32)
+      if (r < rows) acc = fma(col[r], ws[r], acc);
+    acc = warp_sum_t<T>(acc);
+    if (lane == 0) red[i] = (double)acc;
+  }
+  __syncthreads();
+  finish_columns(red, ncols, b, c, nchunks, partials, counters, out, out_bstride, 1, 1);
 }
 
 // ---------------------------------------------------------------------------
@@ -366,12 +527,72 @@ int launch_proj(const T *Q, int64_t q_bstride, int64_t q_istride, int ncols, con
                 double *out, int64_t out_bstride, int64_t out_istride, cudaStream_t s) {
   if (ncols <= 0 || p <= 0) return MFG_OK;
   const int64_t nch = num_chunks<T>(n);
-  if (p > 65535) return MFG_ERR_UNSUPPORTED;
+  if (p > 65535 || ncols > kMaxProjCols) return MFG_ERR_UNSUPPORTED;
   dim3 grid((unsigned)nch, (unsigned)p);
-  proj_kernel<T><<<grid, kThreads, 0, s>>>(Q, q_bstride, q_istride, ncols, Wv, w_bstride, n,
-                                           (int)nch, partials, counters, out, out_bstride,
-                                           out_istride);
+  const size_t smem = (size_t)ncols * kWarps * sizeof(double);
+  proj_kernel<T><<<grid, kThreads, smem, s>>>(Q, q_bstride, q_istride, ncols, Wv, w_bstride, n,
+                                              (int)nch, partials, counters, out, out_bstride,
+                                              out_istride);
   return cudaGetLastError() == cudaSuccess ? MFG_OK : MFG_ERR_CUDA;
+}
+
+// Rows per CTA of the fused kernel: the largest of 4/2/1 rows per thread
+// (width-limited for doubles) whose basis tile fits the shared-memory budget.
+// shared memory of the fused kernel: basis tile, w' tile, coefficients, column sums
+template <typename T>
+static size_t sub_proj_smem(int ncols, int64_t R) {
+  return (size_t)ncols * R * sizeof(T) + (size_t)R * sizeof(T) + (size_t)(ncols + 2) * sizeof(T) +
+         (size_t)ncols * sizeof(double);
+}
+
+template <typename T>
+int sub_proj_rows_per_thread(int ncols) {
+  if (ncols > kMaxProjCols) return 0;
+  for (int ept = (sizeof(T) == 4 ? 4 : 2); ept >= 1; ept >>= 1)
+    if (sub_proj_smem<T>(ncols, (int64_t)kThreads * ept) <= kSubProjSmemBudget) return ept;
+  return 0;
+}
+
+template <typename T> int64_t max_fused_chunks(int64_t n) { return ceil_div(n, kThreads); }
+
+template <typename T, int EPT>
+static int launch_sub_proj_t(const T *Q, int64_t q_bstride, int64_t q_istride, int ncols,
+                             const double *coef, int64_t c_bstride, int64_t c_istride, T *Wv,
+                             int64_t w_bstride, int64_t n, int64_t p, double *partials,
+                             unsigned *counters, double *out, int64_t out_bstride, int *status,
+                             cudaStream_t s) {
+  const int64_t R = (int64_t)kThreads * EPT;
+  const int64_t nch = ceil_div(n, R);
+  const size_t smem = sub_proj_smem<T>(ncols, R);
+  if (smem > 48 * 1024)
+    MFG_CUDA_TRY(cudaFuncSetAttribute(sub_proj_kernel<T, EPT>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  dim3 grid((unsigned)nch, (unsigned)p);
+  sub_proj_kernel<T, EPT><<<grid, kThreads, smem, s>>>(Q, q_bstride, q_istride, ncols, coef,
+                                                       c_bstride, c_istride, Wv, w_bstride, n,
+                                                       (int)nch, partials, counters, out,
+                                                       out_bstride, status);
+  return cudaGetLastError() == cudaSuccess ? MFG_OK : MFG_ERR_CUDA;
+}
+
+template <typename T>
+int launch_sub_proj(const T *Q, int64_t q_bstride, int64_t q_istride, int ncols, const double *coef,
+                    int64_t c_bstride, int64_t c_istride, T *Wv, int64_t w_bstride, int64_t n,
+                    int64_t p, double *partials, unsigned *counters, double *out,
+                    int64_t out_bstride, int *status, cudaStream_t s) {
+  if (ncols <= 0 || p <= 0) return MFG_OK;
+  if (p > 65535) return MFG_ERR_UNSUPPORTED;
+  const int ept = sub_proj_rows_per_thread<T>(ncols);
+  if (ept == 4)
+    return launch_sub_proj_t<T, 4>(Q, q_bstride, q_istride, ncols, coef, c_bstride, c_istride, Wv,
+                                   w_bstride, n, p, partials, counters, out, out_bstride, status, s);
+  if (ept == 2)
+    return launch_sub_proj_t<T, 2>(Q, q_bstride, q_istride, ncols, coef, c_bstride, c_istride, Wv,
+                                   w_bstride, n, p, partials, counters, out, out_bstride, status, s);
+  if (ept == 1)
+    return launch_sub_proj_t<T, 1>(Q, q_bstride, q_istride, ncols, coef, c_bstride, c_istride, Wv,
+                                   w_bstride, n, p, partials, counters, out, out_bstride, status, s);
+  return MFG_ERR_UNSUPPORTED;
 }
 
 template <typename T>
@@ -420,6 +641,11 @@ int launch_inv(const double *x, double *y, int64_t p, cudaStream_t s) {
 }
 
 #define MFG_INST(T)                                                                          \
+  template int sub_proj_rows_per_thread<T>(int);                                               \
+  template int64_t max_fused_chunks<T>(int64_t);                                               \
+  template int launch_sub_proj<T>(const T *, int64_t, int64_t, int, const double *, int64_t,   \
+                                  int64_t, T *, int64_t, int64_t, int64_t, double *,           \
+                                  unsigned *, double *, int64_t, int *, cudaStream_t);         \
   template int launch_proj<T>(const T *, int64_t, int64_t, int, const T *, int64_t, int64_t,   \
                               int64_t, double *, unsigned *, double *, int64_t, int64_t,       \
                               cudaStream_t);                                                   \

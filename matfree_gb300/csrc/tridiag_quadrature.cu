@@ -65,7 +65,9 @@ __global__ void tridiag_ql_kernel(int k, int64_t p, const double *__restrict__ H
       for (int i = m - 1; i >= l; --i) {
         const double f = s * E_(i);
         const double bb = c * E_(i);
-        r = hypot(f, g);
+        // entries of Lanczos tridiagonals are far from the overflow range,
+        // so the plain Euclidean norm replaces hypot; one reciprocal per rotation
+        r = sqrt(f * f + g * g);
         E_(i + 1) = r;
         if (r == 0.0) {  // split: recover and restart the sweep
           D_(i + 1) -= shift_acc;
@@ -73,8 +75,9 @@ __global__ void tridiag_ql_kernel(int k, int64_t p, const double *__restrict__ H
           deflated = true;
           break;
         }
-        s = f / r;
-        c = g / r;
+        const double rinv = 1.0 / r;
+        s = f * rinv;
+        c = g * rinv;
         g = D_(i + 1) - shift_acc;
         r = (D_(i) - g) * s + 2.0 * c * bb;
         shift_acc = s * r;
@@ -136,7 +139,15 @@ int launch_tridiag_quadrature(int64_t k, int64_t p, const double *H, int32_t fun
   const size_t per_thread = (size_t)3 * k * sizeof(double);
   const size_t budget = 48 * 1024;
   if (per_thread > budget) return MFG_ERR_UNSUPPORTED;
-  int tb = 32;
+  // The solve is a serial float64 chain per problem: spread the problems over
+  // all SMs (a few threads per CTA) so that no SM's float64 pipe is shared
+  // by many of them.
+  int sms = 152;
+  int dev = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess)
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int tb = 1;
+  while (tb < 32 && (int64_t)tb * sms < p) tb <<= 1;
   while (tb > 1 && (size_t)tb * per_thread > budget) tb >>= 1;
   const unsigned grid = (unsigned)ceil_div(p, tb);
   tridiag_ql_kernel<<<grid, tb, (size_t)tb * per_thread, s>>>((int)k, p, H, fun, param, scale,

@@ -262,7 +262,7 @@ class CallbackOperator(Operator):
 def as_operator(matvec, n: int, dtype=torch.float32, params=()) -> Operator:
     """Return ``matvec`` as an operator descriptor (wrapping callables)."""
     if isinstance(matvec, CallbackOperator):
-        return matvec.with_params(params)
+        return matvec.with_params(params) if params else matvec
     if isinstance(matvec, Operator):
         if matvec.n != n:
             raise ValueError(f"operator dimension {matvec.n} does not match vector length {n}")

@@ -312,3 +312,41 @@ def test_funm_lanczos_sym_logm_vector():
     w, U = np.linalg.eigh(A)
     want = U @ (np.log(w) * (U.T @ v))
     np.testing.assert_allclose(got, want, rtol=1e-6, atol=1e-8)
+
+
+# ------------------------------------------------------- tensor-core apply
+
+
+@pytest.mark.parametrize("precision,tol", [("bf16x3", 5e-5), ("bf16", 1.5e-2)])
+@pytest.mark.parametrize("n,p", [(64, 16), (200, 1), (300, 100), (1000, 256), (777, 300)])
+def test_dense_tensor_core_apply(precision, tol, n, p):
+    rng = np.random.default_rng(n + p)
+    A = rng.standard_normal((n, n)) / np.sqrt(n)
+    V = rng.standard_normal((p, n))
+    op = mf.DenseOperator(_t(A, torch.float32), precision=precision, shift=0.5)
+    W = op.matmat(_t(V, torch.float32)).double().cpu().numpy()
+    A32 = A.astype(np.float32).astype(np.float64)
+    V32 = V.astype(np.float32).astype(np.float64)
+    want = V32 @ A32.T + 0.5 * V32
+    err = np.abs(W - want).max() / np.abs(want).max()
+    assert err < tol, err
+
+
+@pytest.mark.parametrize("precision,tol", [("bf16x3", 1e-4), ("fp32", 1e-4), ("bf16", 3e-3)])
+def test_slq_rbf_precisions_vs_fp64(precision, tol):
+    n, k, p = 2048, 40, 32
+    x = problems.rbf_points(n, seed=0).astype(np.float32)
+    op = mf.RBFKernelOperator(_t(x, torch.float32), precision=precision)
+    key = mf.prng.prng_key(5)
+    V = philox.rademacher(key, p, n)
+    integrand = mf.funm.monte_carlo_funm_sym_logdet(mf.decomp.tridiag_sym(k))
+    got = float(integrand.batched(op, _t(V, torch.float32)).mean())
+    if precision == "bf16":
+        # Plain bf16 storage perturbs K by ~2^-9 per entry, far more than the
+        # 1e-2 nugget tolerates; parity is checked against float64 SLQ of the
+        # operator as stored (bf16 entries + exact nugget), on the same probes.
+        K = op.dense().cpu().numpy()
+    else:
+        K = problems.rbf_kernel(x.astype(np.float64))
+    want = slq.slq_batched(lambda X: X @ K, k, V).mean()
+    assert abs(got - want) <= tol * abs(want), (got, want, abs(got - want) / abs(want))
