@@ -35,6 +35,9 @@ if ROOT not in sys.path:
 CONFIGS = {
     # name: (kind, n, k, p)
     "rbf16k": ("rbf", 16384, 64, 256),
+    # small case of the same kernels for ncu captures (operator 268 MB and
+    # basis 134 MB: both above L2)
+    "rbf8k": ("rbf", 8192, 16, 256),
     "dense1k": ("dense", 1000, 30, 100),
     "laplace1m": ("csr", 1024 * 1024, 100, 64),
 }

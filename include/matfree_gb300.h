@@ -127,6 +127,26 @@ MFG_API int mfg_hessenberg(const mfg_operator *op, int64_t k, int64_t p, const v
                    double *init_len_inv, void *workspace, size_t workspace_bytes,
                    void *stream);
 
+/* Bytes of workspace mfg_hessenberg_adjoint needs. */
+MFG_API size_t mfg_adjoint_workspace_bytes(const mfg_operator *op, int64_t k, int64_t p, int64_t ld);
+
+/* Reverse pass of mfg_hessenberg for p probes (the Hessenberg adjoint of
+ * Kraemer et al. 2024) with cotangents dH (p k x k float64), optional dr
+ * (p rows of ld) and dc (p float64); the cotangent of Q must be zero, which
+ * holds for every integrand that reads only T.  Inputs are the forward
+ * outputs Q, H, residual and init_len_inv.  Outputs: dv (p rows of ld), the
+ * cotangent of the starting vectors, and Lambda (p*k rows of ld, layout of
+ * Q), the adjoint states lambda_idx of every step, from which the caller
+ * forms parameter gradients sum_idx lambda_idx^T (dA/dtheta) q_idx.  The
+ * operator must be symmetric (A^T lambda is evaluated as A lambda).
+ * Replaces decomp._hessenberg_adjoint / _hessenberg_adjoint_step
+ * (matfree/decomp.py:480-600); k = 0 returns MFG_ERR_RANGE (decomp.py:483-486). */
+MFG_API int mfg_hessenberg_adjoint(const mfg_operator *op, int64_t k, int64_t p, int64_t ld,
+                                   const void *Q, const double *H, const void *residual,
+                                   const double *init_len_inv, const double *dH, const void *dr,
+                                   const double *dc, void *Lambda, void *dv, void *workspace,
+                                   size_t workspace_bytes, void *stream);
+
 /* For each of p Hessenberg matrices: T = (H + H^T)/2 restricted to its
  * tridiagonal part, eigenvalues by implicit QL in float64 with the first
  * eigenvector components tracked (Golub-Welsch), and
@@ -157,6 +177,13 @@ MFG_API int mfg_slq(const mfg_operator *op, int64_t k, int64_t p, const void *pr
  * tutorials/8_gaussian_logpdf.py:21-30. */
 MFG_API int mfg_rbf_build(const float *x, int64_t n, int32_t dim, double s2, double ell,
                   int32_t precision, void *a, void *a_lo, int64_t lda, void *stream);
+
+/* The derivative of the same matrix with respect to log(ell):
+ * s2 exp(-|x_i - x_j|^2 / (2 ell^2)) |x_i - x_j|^2 / ell^2, same storage
+ * options; the operator that contracts adjoint states for d logdet / d log ell
+ * (the parameter part of the matvec VJP in matfree/decomp.py:587-589). */
+MFG_API int mfg_rbf_build_dlogell(const float *x, int64_t n, int32_t dim, double s2, double ell,
+                                  int32_t precision, void *a, void *a_lo, int64_t lda, void *stream);
 
 /* Split a float32 matrix into bf16 hi = bf16(a) and lo = bf16(a - hi). */
 /* ---- launch accounting (diagnostics) ------------------------------------ */

@@ -61,7 +61,10 @@ SIGNATURES = {
     "mfg_tridiag_quadrature": (c_int, [c_int64, c_int64, c_void_p, c_int32, c_double, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     "mfg_slq": (c_int, [POINTER(MfgOperator), c_int64, c_int64, c_void_p, c_int64, c_int32, c_double, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
     "mfg_rbf_build": (c_int, [c_void_p, c_int64, c_int32, c_double, c_double, c_int32, c_void_p, c_void_p, c_int64, c_void_p]),
+    "mfg_rbf_build_dlogell": (c_int, [c_void_p, c_int64, c_int32, c_double, c_double, c_int32, c_void_p, c_void_p, c_int64, c_void_p]),
     "mfg_split_bf16": (c_int, [c_void_p, c_int64, c_int64, c_int64, c_void_p, c_void_p, c_int64, c_void_p]),
+    "mfg_adjoint_workspace_bytes": (c_size_t, [POINTER(MfgOperator), c_int64, c_int64, c_int64]),
+    "mfg_hessenberg_adjoint": (c_int, [POINTER(MfgOperator), c_int64, c_int64, c_int64, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
     "mfg_profile_enable": (c_int, [c_int]),
     "mfg_profile_read": (c_int, [c_int32, POINTER(c_double), POINTER(c_double), POINTER(c_double), POINTER(c_int64)]),
 }

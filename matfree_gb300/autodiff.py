@@ -1,0 +1,191 @@
+"""Gradients of SLQ estimates with respect to operator hyper-parameters.
+
+The reverse pass mirrors what JAX differentiates in matfree:
+
+1. the quadrature ``||v||^2 e1^T f(T) e1`` (funm.py:239-241) through the
+   symmetric eigendecomposition of T (funm.py:330-333): the Daleckii-Krein
+   formula gives d/dT = S (F o s1 s1^T) S^T with F the divided differences
+   of f at the eigenvalues (f' on the diagonal);
+2. T = tridiagonal part of (H + H^T)/2 (decomp.py:133-135, 148-152) -> dH;
+3. the Hessenberg adjoint (decomp.py:480-600) on the GPU
+   (``mfg_hessenberg_adjoint``), which returns the adjoint states Lambda;
+4. the parameter part of each step's matvec VJP, summed over steps and
+   probes: sum lambda_idx^T (dA/dtheta) q_idx = <Lambda, (dA/dtheta) Q>,
+   evaluated for all steps at once by applying dA/dtheta to the stacked
+   Krylov basis (one tensor-core operator application per parameter).
+
+Step 1 runs as batched torch linear algebra on the GPU on p small k x k
+matrices; everything of size n runs in the CUDA library.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import math
+
+import torch
+
+from . import _lib
+from ._panel import Workspace, as_panel, padded_ld, require_cuda, stream_ptr
+from .decomp import _tridiag_from_hessenberg, run_hessenberg
+from .operators import DenseOperator, RBFKernelOperator
+
+_WS = Workspace()
+
+
+def quadform_dH(H: torch.Tensor, scale: torch.Tensor, f, fprime) -> tuple[torch.Tensor, torch.Tensor]:
+    """Values scale_b e1^T f(T_b) e1 and their cotangent with respect to H.
+
+    H: (p, k, k) float64; scale: (p,) float64.  Returns (values (p,), dH (p, k, k)).
+    """
+    d, e = _tridiag_from_hessenberg(H)
+    p, k = d.shape
+    T = torch.diag_embed(d) + torch.diag_embed(e, 1) + torch.diag_embed(e, -1)
+    w, S = torch.linalg.eigh(T)
+    fw = f(w)
+    s1 = S[:, 0, :]
+    values = scale * (fw * s1 * s1).sum(-1)
+    diff = w[:, :, None] - w[:, None, :]
+    same = diff.abs() <= 1e-13 * torch.clamp(w.abs()[:, :, None], min=1.0)
+    F = (fw[:, :, None] - fw[:, None, :]) / torch.where(same, torch.ones_like(diff), diff)
+    F = torch.where(same, fprime(0.5 * (w[:, :, None] + w[:, None, :])), F)
+    G = S @ (F * s1[:, :, None] * s1[:, None, :]) @ S.transpose(-1, -2)
+    G = G * scale[:, None, None]
+    # T_dense = diag(d) + diag(e, 1) + diag(e, -1), d = diag(H), e = (H[i,i+1] + H[i+1,i])/2
+    dH = torch.zeros_like(H)
+    i = torch.arange(k, device=H.device)
+    dH[:, i, i] = G[:, i, i]
+    if k > 1:
+        de = G[:, i[:-1], i[1:]] + G[:, i[1:], i[:-1]]
+        dH[:, i[:-1], i[1:]] = 0.5 * de
+        dH[:, i[1:], i[:-1]] = 0.5 * de
+    return values, dH
+
+
+def hessenberg_adjoint(op, Q, H, R, c, dH, dr=None, dc=None):
+    """GPU reverse pass.  Q (p, k, ld) / R (p, ld) are the forward panels.
+
+    Returns (Lambda (p, k, ld), dv (p, ld)).
+    """
+    p, k, ld = Q.shape
+    if k == 0:
+        # matfree/decomp.py:483-486
+        raise ValueError("Custom Hessenberg-adjoints are not implemented for num_matvecs = 0.")
+    Lam = torch.zeros_like(Q)
+    dv = torch.zeros_like(R)
+    s = op.c_struct()
+    lib = _lib.lib()
+    nbytes = lib.mfg_adjoint_workspace_bytes(ctypes.byref(s), k, p, ld)
+    ws, wsb = _WS.get(nbytes, Q.device)
+    vp = lambda t: ctypes.c_void_p(t.data_ptr()) if t is not None else ctypes.c_void_p(0)  # noqa: E731
+    st = lib.mfg_hessenberg_adjoint(ctypes.byref(s), k, p, ld, vp(Q), vp(H.contiguous()), vp(R), vp(c),
+                                    vp(dH.contiguous()), vp(dr), vp(dc), vp(Lam), vp(dv), ws, wsb,
+                                    stream_ptr())
+    _lib.check(st, "mfg_hessenberg_adjoint")
+    return Lam, dv
+
+
+def _log(x):
+    return torch.log(x)
+
+
+def _dlog(x):
+    return 1.0 / x
+
+
+class _RBFLogdet(torch.autograd.Function):
+    """mean_b ||v_b||^2 e1^T log(T_b) e1 for K(theta), differentiable in theta."""
+
+    @staticmethod
+    def forward(ctx, theta, x, probes, k, precision):
+        s2, ell, tau = (float(math.exp(t)) for t in theta.detach().cpu().tolist())
+        op = RBFKernelOperator(x, s2=s2, ell=ell, tau=tau, precision=precision)
+        n = op.n
+        panel, ld = as_panel(probes, n, op.basis_dtype)
+        p = panel.shape[0]
+        Q, H, R, c = _forward_panels(op, k, panel, ld)
+        scale = 1.0 / (c * c)
+        values, dH = quadform_dH(H, scale, _log, _dlog)
+        ctx.save_for_backward(theta, x)
+        ctx.saved = (op, Q, H, R, c, dH, p, precision)
+        return values.mean()
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        theta, x = ctx.saved_tensors
+        op, Q, H, R, c, dH, p, precision = ctx.saved
+        dH = dH * (grad_out.double() / p)
+        Lam, _dv = hessenberg_adjoint(op, Q, H, R, c, dH)
+        grad = rbf_theta_contractions(op, x, Q, Lam)
+        return grad.to(theta.dtype), None, None, None, None
+
+
+def _forward_panels(op, k, panel, ld):
+    """mfg_hessenberg keeping the padded (p, k, ld) / (p, ld) panels."""
+    p = panel.shape[0]
+    dt = op.basis_dtype
+    Q = torch.zeros((p, k, ld), dtype=dt, device=panel.device)
+    H = torch.zeros((p, k, k), dtype=torch.float64, device=panel.device)
+    R = torch.zeros((p, ld), dtype=dt, device=panel.device)
+    c = torch.zeros((p,), dtype=torch.float64, device=panel.device)
+    s = op.c_struct()
+    lib = _lib.lib()
+    nbytes = lib.mfg_slq_workspace_bytes(ctypes.byref(s), k, p, ld)
+    ws, wsb = _WS.get(nbytes, panel.device)
+    st = lib.mfg_hessenberg(ctypes.byref(s), k, p, ctypes.c_void_p(panel.data_ptr()), ld, 1,
+                            ctypes.c_void_p(Q.data_ptr()), ctypes.c_void_p(H.data_ptr()),
+                            ctypes.c_void_p(R.data_ptr()), ctypes.c_void_p(c.data_ptr()), ws, wsb,
+                            stream_ptr())
+    _lib.check(st, "mfg_hessenberg")
+    return Q, H, R, c
+
+
+def rbf_theta_contractions(op: RBFKernelOperator, x, Q, Lam) -> torch.Tensor:
+    """d/dtheta of sum_idx lambda_idx^T K(theta) q_idx for theta = (log s2, log ell, log tau).
+
+    dK/dlog s2 = K - tau I,  dK/dlog ell = s2 E o D / ell^2,  dK/dlog tau = tau I.
+    """
+    p, k, ld = Q.shape
+    n = op.n
+    rows = Q.reshape(p * k, ld)[:, :n]
+    lam = Lam.reshape(p * k, ld)[:, :n].double()
+    # the stored exponential part (without the nugget) is dK/dlog s2
+    base = DenseOperator._from_storage(n, op.precision, op.a, op.a_lo, 0.0)
+    g0 = (lam * base.matmat(rows).double()).sum()
+    dl = _rbf_dlogell_operator(op, x)
+    g1 = (lam * dl.matmat(rows).double()).sum()
+    g2 = op.tau * (lam * rows.double()).sum()
+    return torch.stack([g0, g1, g2])
+
+
+def _rbf_dlogell_operator(op: RBFKernelOperator, x) -> DenseOperator:
+    lda = padded_ld(op.n)
+    dt = op.a.dtype
+    a = torch.empty((op.n, lda), dtype=dt, device=x.device)
+    a_lo = torch.empty((op.n, lda), dtype=dt, device=x.device) if op.precision == "bf16x3" else None
+    st = _lib.lib().mfg_rbf_build_dlogell(
+        ctypes.c_void_p(op.x.data_ptr()), op.n, op.dim, op.s2, op.ell, _lib.PRECISIONS[op.precision],
+        ctypes.c_void_p(a.data_ptr()), ctypes.c_void_p(a_lo.data_ptr() if a_lo is not None else 0), lda,
+        stream_ptr())
+    _lib.check(st, "mfg_rbf_build_dlogell")
+    return DenseOperator._from_storage(op.n, op.precision, a, a_lo, 0.0)
+
+
+def rbf_logdet(x: torch.Tensor, theta: torch.Tensor, probes: torch.Tensor, num_matvecs: int,
+               precision: str = "bf16x3") -> torch.Tensor:
+    """SLQ estimate of log det K(theta) on the given probes, differentiable in theta.
+
+    theta = (log s2, log ell, log tau) as a CUDA or CPU tensor of 3 values;
+    probes (p, n) CUDA tensor; returns a 0-d float64 tensor.
+    """
+    require_cuda(x, "x")
+    require_cuda(probes, "probes")
+    if num_matvecs <= 0 or num_matvecs > x.shape[0]:
+        from .decomp import _error_num_matvecs
+
+        raise ValueError(_error_num_matvecs(num_matvecs, maxval=x.shape[0], minval=0))
+    return _RBFLogdet.apply(theta, x.to(torch.float32).contiguous(), probes, int(num_matvecs), precision)
+
+
+__all__ = ["quadform_dH", "hessenberg_adjoint", "rbf_logdet", "rbf_theta_contractions",
+           "run_hessenberg"]

@@ -297,6 +297,143 @@ static int run_hessenberg(const mfg_operator *op, int64_t k, int64_t p, const T 
   return MFG_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Batched Hessenberg adjoint (reverse Arnoldi), matfree/decomp.py:480-600.
+// ---------------------------------------------------------------------------
+
+struct AdjLayout {
+  size_t lam, lam2, U, panel, h, g, coef, bp, gamma, scal, beta, Gamma, Pi, inv, partials,
+      counters, status, hi, lo, total;
+};
+
+static AdjLayout adj_layout(const mfg_operator *op, int64_t k, int64_t p, int64_t ld) {
+  AdjLayout L{};
+  const size_t es = (size_t)elem_size_for(op);
+  const int64_t nch = es == 8 ? max_fused_chunks<double>(op->n) : max_fused_chunks<float>(op->n);
+  const int64_t kk = k > 0 ? k : 1;
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    const size_t o = off;
+    off = align_up(off + bytes, 256);
+    return o;
+  };
+  L.lam = take((size_t)p * ld * es);
+  L.lam2 = take((size_t)p * ld * es);
+  L.U = take((size_t)p * ld * es);
+  L.panel = take(op->kind == MFG_OP_CALLBACK ? (size_t)p * ld * es : 0);
+  L.h = take((size_t)p * kk * 8);
+  L.g = take((size_t)p * kk * 8);
+  L.coef = take((size_t)p * kk * 8);
+  L.bp = take((size_t)p * kk * 8);
+  L.gamma = take((size_t)p * kk * 8);
+  L.scal = take((size_t)p * 3 * 8);
+  L.beta = take((size_t)p * 8);
+  L.Gamma = take((size_t)p * kk * kk * 8);
+  L.Pi = take((size_t)p * kk * kk * 8);
+  L.inv = take((size_t)p * 8);
+  L.partials = take((size_t)p * nch * (kk + 1) * 8);
+  L.counters = take((size_t)p * 4);
+  L.status = take(16);
+  L.hi = take(uses_bf16(op) ? (size_t)p * ld * 2 : 0);
+  L.lo = take(uses_bf16(op) && op->precision == MFG_PREC_BF16X3 ? (size_t)p * ld * 2 : 0);
+  L.total = off + 256;
+  return L;
+}
+
+template <typename T>
+static int run_adjoint(const mfg_operator *op, int64_t k, int64_t p, int64_t ld, const T *Q,
+                       const double *H, const T *R, const double *c, const double *dH, const T *dr,
+                       const double *dc, T *Lam, T *dv, const AdjLayout &L, char *ws,
+                       cudaStream_t s) {
+  const int64_t n = op->n;
+  const int64_t qb = k * ld;
+  T *lam = reinterpret_cast<T *>(ws + L.lam);
+  T *lam2 = reinterpret_cast<T *>(ws + L.lam2);
+  T *U = reinterpret_cast<T *>(ws + L.U);
+  T *panel = reinterpret_cast<T *>(ws + L.panel);
+  double *h = reinterpret_cast<double *>(ws + L.h);
+  double *g = reinterpret_cast<double *>(ws + L.g);
+  double *coef = reinterpret_cast<double *>(ws + L.coef);
+  double *bp = reinterpret_cast<double *>(ws + L.bp);
+  double *gamma = reinterpret_cast<double *>(ws + L.gamma);
+  double *scal = reinterpret_cast<double *>(ws + L.scal);
+  double *beta = reinterpret_cast<double *>(ws + L.beta);
+  double *Gamma = reinterpret_cast<double *>(ws + L.Gamma);
+  double *Pi = reinterpret_cast<double *>(ws + L.Pi);
+  double *inv = reinterpret_cast<double *>(ws + L.inv);
+  double *partials = reinterpret_cast<double *>(ws + L.partials);
+  unsigned *counters = reinterpret_cast<unsigned *>(ws + L.counters);
+  int *status = reinterpret_cast<int *>(ws + L.status);
+  __nv_bfloat16 *hi = uses_bf16(op) ? reinterpret_cast<__nv_bfloat16 *>(ws + L.hi) : nullptr;
+  __nv_bfloat16 *lo = (uses_bf16(op) && op->precision == MFG_PREC_BF16X3)
+                          ? reinterpret_cast<__nv_bfloat16 *>(ws + L.lo)
+                          : nullptr;
+  const double vecb = (double)n * (double)p * (double)sizeof(T);
+  double ab = 0.0, af = 0.0;
+  apply_cost(op, p, &ab, &af);
+
+  MFG_CUDA_TRY(cudaMemsetAsync(counters, 0, (size_t)p * 4, s));
+  MFG_CUDA_TRY(cudaMemsetAsync(status, 0, 16, s));
+  MFG_CUDA_TRY(cudaMemsetAsync(Gamma, 0, (size_t)p * k * k * 8, s));
+  MFG_CUDA_TRY(cudaMemsetAsync(lam, 0, (size_t)p * ld * sizeof(T), s));
+  MFG_LAUNCH(MFG_PROF_OTHER, 24.0 * p * k * k, 2.0 * p * k * k * k,
+             launch_pi_gamma(H, dH, dc, c, (int)k, p, Pi, s));
+  // gamma = dH e_K - Q^T dr ;  lambda = dr + Q gamma   (decomp.py:498-499)
+  if (dr) {
+    MFG_LAUNCH(MFG_PROF_PROJ, (k + 1.0) * vecb, 2.0 * k * vecb / sizeof(T),
+               launch_proj<T>(Q, qb, ld, (int)k, dr, ld, n, p, partials, counters, h, k, 1, s));
+    MFG_CUDA_TRY(cudaMemcpy2DAsync(lam, ld * sizeof(T), dr, ld * sizeof(T), ld * sizeof(T), p,
+                                   cudaMemcpyDeviceToDevice, s));
+  }
+  MFG_LAUNCH(MFG_PROF_OTHER, 16.0 * p * k, (double)p * k,
+             launch_adj_init(dH, dr ? h : nullptr, (int)k, p, gamma, coef, s));
+  MFG_LAUNCH(MFG_PROF_SUB, (k + 2.0) * vecb, 2.0 * k * vecb / sizeof(T),
+             launch_sub<T>(Q, qb, ld, (int)k, coef, k, 1, lam, lam, ld, n, p, false, true, partials,
+                           counters, nullptr, nullptr, 0, s));
+
+  for (int64_t idx = k - 1; idx >= 0; --idx) {
+    const int ncr = (int)(idx + 2 < k ? idx + 2 : k);
+    // masked re-projection: lambda -= Q_m (Q_m^T lambda - dH[:, idx]_m)   (decomp.py:576-584)
+    MFG_LAUNCH(MFG_PROF_PROJ, (ncr + 1.0) * vecb, 2.0 * ncr * vecb / sizeof(T),
+               launch_proj<T>(Q, qb, ld, ncr, lam, ld, n, p, partials, counters, h, k, 1, s));
+    MFG_LAUNCH(MFG_PROF_OTHER, 16.0 * p * ncr, (double)p * ncr,
+               launch_adj_reortho_coef(h, dH, (int)k, p, (int)idx, ncr, coef, s));
+    MFG_LAUNCH(MFG_PROF_SUB, (ncr + 2.0) * vecb, 2.0 * ncr * vecb / sizeof(T),
+               launch_sub<T>(Q, qb, ld, ncr, coef, k, 1, lam, lam, ld, n, p, false, true, partials,
+                             counters, nullptr, nullptr, 0, s));
+    // U = A^T lambda (= A lambda: tridiag_sym's operators are symmetric)   (decomp.py:587-589)
+    if (hi) MFG_TRY(launch_split_bf16((const float *)lam, p, n, ld, hi, lo, ld, s));
+    MFG_LAUNCH(MFG_PROF_APPLY, ab, af, apply_op<T>(op, lam, ld, U, ld, p, hi, lo, ld, panel, status, s));
+    // Gamma row idx, (Gamma + Gamma^T)[idx, :], beta_plus row   (decomp.py:592-599)
+    MFG_LAUNCH(MFG_PROF_PROJ, (idx + 2.0) * vecb, 2.0 * (idx + 1.0) * vecb / sizeof(T),
+               launch_proj<T>(Q, qb, ld, (int)(idx + 1), U, ld, n, p, partials, counters, g, k, 1, s));
+    MFG_LAUNCH(MFG_PROF_OTHER, 40.0 * p * k, 4.0 * p * k,
+               launch_adj_step_coef(H, Pi, g, gamma, (int)k, p, (int)idx, Gamma, coef, bp, scal,
+                                    beta, s));
+    MFG_CUDA_TRY(cudaMemcpy2DAsync(Lam + idx * ld, qb * sizeof(T), lam, ld * sizeof(T),
+                                   ld * sizeof(T), p, cudaMemcpyDeviceToDevice, s));
+    // lambda = (gamma_idx r + Q G - alpha lambda + U - Lambda beta_plus) / beta_minus
+    MFG_LAUNCH(MFG_PROF_SCALE, 4.0 * vecb, 3.0 * vecb / sizeof(T),
+               launch_adj_lincomb<T>(U, lam, R, scal, n, ld, p, lam2, s));
+    MFG_LAUNCH(MFG_PROF_SUB, (k + 2.0) * vecb, 2.0 * k * vecb / sizeof(T),
+               launch_sub<T>(Q, qb, ld, (int)k, coef, k, 1, lam2, lam2, ld, n, p, false, true,
+                             partials, counters, nullptr, nullptr, 0, s));
+    if (idx + 1 < k) {
+      const int nb = (int)(k - idx - 1);
+      MFG_LAUNCH(MFG_PROF_SUB, (nb + 2.0) * vecb, 2.0 * nb * vecb / sizeof(T),
+                 launch_sub<T>(Lam + (idx + 1) * ld, qb, ld, nb, bp + idx + 1, k, 1, lam2, lam2, ld,
+                               n, p, false, true, partials, counters, nullptr, nullptr, 0, s));
+    }
+    MFG_LAUNCH(MFG_PROF_SCALE, 2.0 * vecb, vecb / sizeof(T),
+               launch_scale<T>(lam2, ld, n, p, beta, lam, ld, nullptr, nullptr, 0, s));
+  }
+  // dv = lambda c   (decomp.py:541)
+  MFG_LAUNCH(MFG_PROF_OTHER, 16.0 * p, (double)p, launch_inv(c, inv, p, s));
+  MFG_LAUNCH(MFG_PROF_SCALE, 2.0 * vecb, vecb / sizeof(T),
+             launch_scale<T>(lam, ld, n, p, inv, dv, ld, nullptr, nullptr, 0, s));
+  return MFG_OK;
+}
+
 __global__ void square_kernel(const double *x, double *y, int64_t p) {
   const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (b < p) y[b] = x[b] * x[b];
@@ -444,6 +581,35 @@ int mfg_hessenberg(const mfg_operator *op, int64_t k, int64_t p, const void *V, 
                                (float *)residual, init_len_inv, L, ws, s);
 }
 
+size_t mfg_adjoint_workspace_bytes(const mfg_operator *op, int64_t k, int64_t p, int64_t ld) {
+  if (check_op(op) != MFG_OK || k <= 0 || p <= 0 || ld < op->n) return 0;
+  return adj_layout(op, k, p, ld).total;
+}
+
+int mfg_hessenberg_adjoint(const mfg_operator *op, int64_t k, int64_t p, int64_t ld, const void *Q,
+                           const double *H, const void *residual, const double *init_len_inv,
+                           const double *dH, const void *dr, const double *dc, void *Lambda,
+                           void *dv, void *workspace, size_t workspace_bytes, void *stream) {
+  MFG_TRY(check_op(op));
+  MFG_TRY(check_panel(op, p, ld));
+  if (k == 0) return MFG_ERR_RANGE;  // decomp.py:483-486: not defined for num_matvecs = 0
+  if (k < 0 || k > op->n) return MFG_ERR_RANGE;
+  if (!Q || !H || !residual || !init_len_inv || !dH || !Lambda || !dv) return MFG_ERR_BAD_ARG;
+  if (!aligned16(Q) || !aligned16(residual) || !aligned16(Lambda) || !aligned16(dv) ||
+      (dr && !aligned16(dr)))
+    return MFG_ERR_BAD_ARG;
+  const AdjLayout L = adj_layout(op, k, p, ld);
+  if (!workspace || workspace_bytes < L.total) return MFG_ERR_WORKSPACE;
+  char *ws = ws_base(workspace);
+  cudaStream_t s = as_stream(stream);
+  if (op->precision == MFG_PREC_FP64)
+    return run_adjoint<double>(op, k, p, ld, (const double *)Q, H, (const double *)residual,
+                               init_len_inv, dH, (const double *)dr, dc, (double *)Lambda,
+                               (double *)dv, L, ws, s);
+  return run_adjoint<float>(op, k, p, ld, (const float *)Q, H, (const float *)residual, init_len_inv,
+                            dH, (const float *)dr, dc, (float *)Lambda, (float *)dv, L, ws, s);
+}
+
 int mfg_tridiag_quadrature(int64_t k, int64_t p, const double *H, int32_t fun, double param,
                            const double *scale, double *values, double *eigvals, double *first_sq,
                            void *stream) {
@@ -490,16 +656,26 @@ int mfg_slq(const mfg_operator *op, int64_t k, int64_t p, const void *probes, in
   return MFG_OK;
 }
 
-int mfg_rbf_build(const float *x, int64_t n, int32_t dim, double s2, double ell,
-                  int32_t precision, void *a, void *a_lo, int64_t lda, void *stream) {
+static int rbf_build(const float *x, int64_t n, int32_t dim, double s2, double ell,
+                     int32_t precision, int dlogell, void *a, void *a_lo, int64_t lda, void *stream) {
   if (!x || !a || n <= 0 || dim <= 0 || lda < n || lda % 8 != 0 || ell <= 0.0) return MFG_ERR_BAD_ARG;
   if (precision == MFG_PREC_BF16X3 && !a_lo) return MFG_ERR_BAD_ARG;
   if (precision < MFG_PREC_FP32 || precision > MFG_PREC_FP64) return MFG_ERR_BAD_ARG;
   cudaStream_t s = as_stream(stream);
   const double es = precision == MFG_PREC_FP64 ? 8.0 : (precision == MFG_PREC_FP32 ? 4.0 : (precision == MFG_PREC_BF16X3 ? 4.0 : 2.0));
   MFG_LAUNCH(MFG_PROF_OTHER, (double)n * lda * es, 0.0,
-             launch_rbf_build(x, n, dim, s2, ell, precision, a, a_lo, lda, s));
+             launch_rbf_build(x, n, dim, s2, ell, precision, dlogell, a, a_lo, lda, s));
   return MFG_OK;
+}
+
+int mfg_rbf_build(const float *x, int64_t n, int32_t dim, double s2, double ell,
+                  int32_t precision, void *a, void *a_lo, int64_t lda, void *stream) {
+  return rbf_build(x, n, dim, s2, ell, precision, 0, a, a_lo, lda, stream);
+}
+
+int mfg_rbf_build_dlogell(const float *x, int64_t n, int32_t dim, double s2, double ell,
+                          int32_t precision, void *a, void *a_lo, int64_t lda, void *stream) {
+  return rbf_build(x, n, dim, s2, ell, precision, 1, a, a_lo, lda, stream);
 }
 
 int mfg_split_bf16(const float *a, int64_t rows, int64_t cols, int64_t lda, void *hi, void *lo,

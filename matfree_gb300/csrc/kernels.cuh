@@ -33,6 +33,20 @@ int launch_scale(const T *Win, int64_t w_bstride, int64_t n, int64_t p, const do
                  cudaStream_t s);
 int launch_inv(const double *x, double *y, int64_t p, cudaStream_t s);
 
+// adjoint_kernels.cu
+int launch_pi_gamma(const double *H, const double *dH, const double *dc, const double *c, int k,
+                    int64_t p, double *Pi, cudaStream_t s);
+int launch_adj_init(const double *dH, const double *h, int k, int64_t p, double *gamma, double *coef,
+                    cudaStream_t s);
+int launch_adj_reortho_coef(const double *h, const double *dH, int k, int64_t p, int idx, int ncols,
+                            double *coef, cudaStream_t s);
+int launch_adj_step_coef(const double *H, const double *Pi, const double *g, const double *gamma,
+                         int k, int64_t p, int idx, double *Gamma, double *coefG, double *bp,
+                         double *scal, double *beta, cudaStream_t s);
+template <typename T>
+int launch_adj_lincomb(const T *U, const T *lam, const T *R, const double *scal, int64_t n,
+                       int64_t ld, int64_t p, T *out, cudaStream_t s);
+
 // tridiag_quadrature.cu
 int launch_tridiag_quadrature(int64_t k, int64_t p, const double *H, int32_t fun, double param,
                               const double *scale, double *values, double *eigvals,
@@ -47,7 +61,7 @@ int launch_csr_spmm(const int32_t *row_ptr, const int32_t *col_idx, const float 
                     const float *V, int64_t ldv, float *W, int64_t ldw, int64_t p, double shift,
                     cudaStream_t s);
 int launch_rbf_build(const float *x, int64_t n, int dim, double s2, double ell, int precision,
-                     void *a, void *a_lo, int64_t lda, cudaStream_t s);
+                     int dlogell, void *a, void *a_lo, int64_t lda, cudaStream_t s);
 int launch_split_bf16(const float *a, int64_t rows, int64_t cols, int64_t lda, __nv_bfloat16 *hi,
                       __nv_bfloat16 *lo, int64_t ld_out, cudaStream_t s);
 

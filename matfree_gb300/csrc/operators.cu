@@ -195,7 +195,7 @@ int launch_csr_spmm(const int32_t *row_ptr, const int32_t *col_idx, const float 
 
 __global__ void __launch_bounds__(256)
 rbf_kernel(const float *__restrict__ x, int64_t n, int dim, double s2, double inv2l2, int prec,
-           void *__restrict__ a, void *__restrict__ a_lo, int64_t lda) {
+           int dlogell, void *__restrict__ a, void *__restrict__ a_lo, int64_t lda) {
   const int64_t i = blockIdx.y;
   const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= lda) return;
@@ -209,6 +209,7 @@ rbf_kernel(const float *__restrict__ x, int64_t n, int dim, double s2, double in
         d2 += df * df;
       }
       v = s2 * exp(-d2 * inv2l2);
+      if (dlogell) v *= 2.0 * d2 * inv2l2;  // d/dlog(ell) of exp(-d2/(2 ell^2))
     }
     reinterpret_cast<double *>(a)[o] = v;
     return;
@@ -221,6 +222,7 @@ rbf_kernel(const float *__restrict__ x, int64_t n, int dim, double s2, double in
       d2 = fmaf(df, df, d2);
     }
     v = (float)s2 * expf(-d2 * (float)inv2l2);
+    if (dlogell) v *= 2.f * d2 * (float)inv2l2;
   }
   if (prec == MFG_PREC_FP32) {
     reinterpret_cast<float *>(a)[o] = v;
@@ -233,12 +235,12 @@ rbf_kernel(const float *__restrict__ x, int64_t n, int dim, double s2, double in
 }
 
 int launch_rbf_build(const float *x, int64_t n, int dim, double s2, double ell, int precision,
-                     void *a, void *a_lo, int64_t lda, cudaStream_t s) {
+                     int dlogell, void *a, void *a_lo, int64_t lda, cudaStream_t s) {
   if (n <= 0) return MFG_OK;
   if (n > 65535) return MFG_ERR_UNSUPPORTED;
   const double inv2l2 = 1.0 / (2.0 * ell * ell);
   rbf_kernel<<<dim3((unsigned)ceil_div(lda, 256), (unsigned)n), 256, 0, s>>>(
-      x, n, dim, s2, inv2l2, precision, a, a_lo, lda);
+      x, n, dim, s2, inv2l2, precision, dlogell, a, a_lo, lda);
   return cudaGetLastError() == cudaSuccess ? MFG_OK : MFG_ERR_CUDA;
 }
 
