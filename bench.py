@@ -134,21 +134,15 @@ def _dist_init(n_gpus):
 
 
 def _barrier(world):
-    if world > 1:
-        import torch.distributed as dist
+    from matfree_gb300 import replicas
 
-        dist.barrier()
+    replicas.barrier(world)
 
 
 def _max_over_ranks(x, world):
-    if world == 1:
-        return x
-    import torch
-    import torch.distributed as dist
+    from matfree_gb300 import replicas
 
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
+    return replicas.max_over_ranks(x, world)
 
 
 def build_problem(cfg, seed=0):
@@ -378,13 +372,110 @@ def _config(args):
             "l2": "inputs larger than L2 (operator and Krylov basis > 129 MB); no flush"}
 
 
+def grad_arm(args):
+    """log det K(theta) and d/dtheta (RBF n=8192, k=48, p=128) per step."""
+    import torch
+
+    import matfree_gb300 as mf
+    from matfree_gb300 import autodiff
+
+    torch.cuda.set_device(0)
+    n, k, p = 8192, 48, 128
+    x = np.random.default_rng(0).uniform(0.0, 1.0, size=(n, 3)).astype(np.float32)
+    xd = torch.from_numpy(x).cuda()
+    theta0 = np.array([0.0, math.log(0.2), math.log(1e-2)])
+    key = mf.prng.prng_key(1)
+    V = mf.stochtrace.sampler_signs(torch.ones(n, device="cuda"), num=p)(key)
+
+    def step():
+        th = torch.tensor(theta0, dtype=torch.float64, requires_grad=True)
+        val = autodiff.rbf_logdet(xd, th, V, k, precision=args.precision)
+        val.backward()
+        return val.detach(), th.grad
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        val, grad = step()
+    torch.cuda.synchronize()
+    secs = (time.perf_counter() - t0) / args.steps
+    # float64 oracle gradient on the first probes (same probe vectors)
+    from oracle import adjoint as oadj
+    from oracle import philox
+
+    num = args.cpu_probes
+    Vs = philox.rademacher(np.asarray(key, np.uint32), num, n)
+    t1 = time.perf_counter()
+    matmat, vjp_matmat = oadj.rbf_vjp_factory(x.astype(np.float64), theta0)
+    _, g_ref = oadj.slq_grad_batched(matmat, vjp_matmat, 3, k, Vs)
+    cpu_s = time.perf_counter() - t1
+    th = torch.tensor(theta0, dtype=torch.float64, requires_grad=True)
+    autodiff.rbf_logdet(xd, th, V[:num], k, precision=args.precision).backward()
+    g_gpu = th.grad.numpy()
+    rel = np.abs(g_gpu - g_ref) / np.abs(g_ref)
+    line = {"metric": "logdet+grad solves/s", "value": 1.0 / secs, "unit": "solves/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": f"f32 basis / {args.precision} operator / f64 reductions",
+            "data": "synthetic (seeded)",
+            "config": {"workload": f"GP log-det + d/dtheta, RBF n={n}, k={k}, p={p}, theta=(0, log 0.2, log 1e-2)"},
+            "estimate": float(val), "grad": grad.tolist(),
+            "grad_rel_err_vs_fp64_oracle": {"value": rel.tolist(), "on": f"first {num} probes, identical probes"},
+            "cpu_baseline": {"value": 1.0 / (cpu_s * p / num), "unit": "solves/s",
+                             "cores": len(os.sched_getaffinity(0)), "kind": "port",
+                             "sample": f"{num} of {p} probes (float64 forward + adjoint restatement), "
+                                       "extrapolated linearly in probes"}}
+    print(json.dumps(line), flush=True)
+
+
+def serve_arm(args):
+    """Mixed request stream through the continuous-batching server vs one-by-one fp32."""
+    import torch
+
+    from matfree_gb300 import serve
+
+    torch.cuda.set_device(0)
+    reqs = serve.synthetic_stream(args.requests, rate=args.rate, seed=0)
+    warm = serve.synthetic_stream(4, rate=1e6, seed=99)
+    srv = serve.SLQServer(slots=args.slots, budget_bytes=150e9, precision="bf16x3")
+    srv.run(warm, realtime=False)
+    torch.cuda.synchronize()
+    with ClockSampler(0) as clk:
+        res, stats = srv.run(reqs, realtime=True)
+    clocks = clk.summary()
+    plain = serve.SLQServer(slots=1, budget_bytes=150e9, precision="fp32")
+    plain.run(warm[:1], realtime=False)
+    base_reqs = reqs[: args.baseline_requests]
+    _, bstats = plain.run(base_reqs, realtime=False)
+    work = sum(2.0 * r.x.shape[0] ** 2 * r.p * r.k * 3 for r in reqs)
+    line = {"metric": METRIC, "value": stats["solves_per_s"], "unit": UNIT, "n_gpus": 1,
+            "steps": len(reqs), "warmup": len(warm), "ms_per_step": 1e3 * stats["wall_s"] / len(reqs),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 basis / bf16x3 operator / f64 reductions", "data": "synthetic (seeded)",
+            "config": {"workload": f"serving stream: {len(reqs)} RBF log-det / trace-exp requests, Poisson "
+                                   f"arrivals at {args.rate}/s, n log-uniform [512, 32768], k in "
+                                   "{16,32,64,96}, p in {32,64,128,256}, bf16x3 operators built per request",
+                       "slots": args.slots, "budget_gb": 150, "parallelism": "streams"},
+            "latency_ms": {"p50": stats["p50_ms"], "p99": stats["p99_ms"], "mean": stats["mean_ms"]},
+            "plain_fp32_per_request": {"solves_per_s": bstats["solves_per_s"], "requests": len(base_reqs),
+                                       "note": "same requests one at a time, fp32 CUDA-core operator"},
+            "speedup_vs_plain_fp32": stats["solves_per_s"] / bstats["solves_per_s"],
+            "operator_tflop_per_s": work / stats["wall_s"] / 1e12, "clocks": clocks}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="rbf16k", choices=sorted(CONFIGS))
+    ap.add_argument("--config", default="rbf16k", choices=sorted(CONFIGS) + ["serve", "grad8k"])
+    ap.add_argument("--requests", type=int, default=64)
+    ap.add_argument("--baseline-requests", type=int, default=24)
+    ap.add_argument("--rate", type=float, default=150.0)
+    ap.add_argument("--slots", type=int, default=8)
     ap.add_argument("--precision", default="bf16x3", choices=["fp32", "bf16", "bf16x3", "fp64"])
     ap.add_argument("--cpu-probes", type=int, default=8)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -392,6 +483,12 @@ def main():
     if args.warmup < 3:
         args.warmup = 3
 
+    if args.config == "serve" and args.impl == "ours":
+        serve_arm(args)
+        return
+    if args.config == "grad8k" and args.impl == "ours":
+        grad_arm(args)
+        return
     if args.impl == "reference":
         line = reference_arm(args)
         if line is not None:

@@ -96,6 +96,10 @@ MFG_API int mfg_version(void);
 /* Human-readable text of a status code; never NULL. */
 MFG_API const char *mfg_status_string(int status);
 
+/* Where and why the most recent MFG_ERR_CUDA on the calling host thread
+ * arose ("file:line: CUDA error text"); empty if none.  Never NULL. */
+MFG_API const char *mfg_last_error(void);
+
 /* Bytes of workspace the SLQ / tridiagonalisation entry points need. */
 MFG_API size_t mfg_slq_workspace_bytes(const mfg_operator *op, int64_t k, int64_t p, int64_t ld);
 

@@ -53,6 +53,7 @@ class MfgOperator(ctypes.Structure):
 SIGNATURES = {
     "mfg_version": (c_int, []),
     "mfg_status_string": (ctypes.c_char_p, [c_int]),
+    "mfg_last_error": (ctypes.c_char_p, []),
     "mfg_slq_workspace_bytes": (c_size_t, [POINTER(MfgOperator), c_int64, c_int64, c_int64]),
     "mfg_sampler_signs": (c_int, [POINTER(c_uint32), c_int64, c_int64, c_int64, c_int32, c_void_p, c_void_p]),
     "mfg_sampler_normal": (c_int, [POINTER(c_uint32), c_int64, c_int64, c_int64, c_int32, c_void_p, c_void_p]),
@@ -109,4 +110,5 @@ def check(status: int, what: str) -> None:
         raise ValueError(f"{what}: {text}")
     if status == MFG_ERR_BAD_ARG:
         raise ValueError(f"{what}: {text}")
-    raise MatfreeGB300Error(f"{what}: {text} (status {status})")
+    detail = lib().mfg_last_error().decode() if status == MFG_ERR_CUDA else ""
+    raise MatfreeGB300Error(f"{what}: {text} (status {status}) {detail}".rstrip())

@@ -117,7 +117,7 @@ class _RBFLogdet(torch.autograd.Function):
         dH = dH * (grad_out.double() / p)
         Lam, _dv = hessenberg_adjoint(op, Q, H, R, c, dH)
         grad = rbf_theta_contractions(op, x, Q, Lam)
-        return grad.to(theta.dtype), None, None, None, None
+        return grad.to(device=theta.device, dtype=theta.dtype), None, None, None, None
 
 
 def _forward_panels(op, k, panel, ld):

@@ -106,19 +106,19 @@ static inline unsigned blocks(int64_t work, int tb) { return (unsigned)ceil_div(
 int launch_pi_gamma(const double *H, const double *dH, const double *dc, const double *c, int k,
                     int64_t p, double *Pi, cudaStream_t s) {
   pi_gamma_kernel<<<blocks(p * k * k, 128), 128, 0, s>>>(H, dH, dc, c, k, p, Pi);
-  return cudaGetLastError() == cudaSuccess ? MFG_OK : MFG_ERR_CUDA;
+  return MFG_LAUNCH_STATUS();
 }
 
 int launch_adj_init(const double *dH, const double *h, int k, int64_t p, double *gamma, double *coef,
                     cudaStream_t s) {
   adj_init_kernel<<<blocks(p * k, 128), 128, 0, s>>>(dH, h, k, p, gamma, coef);
-  return cudaGetLastError() == cudaSuccess ? MFG_OK : MFG_ERR_CUDA;
+  return MFG_LAUNCH_STATUS();
 }
 
 int launch_adj_reortho_coef(const double *h, const double *dH, int k, int64_t p, int idx, int ncols,
                             double *coef, cudaStream_t s) {
   adj_reortho_coef_kernel<<<blocks(p * ncols, 128), 128, 0, s>>>(h, dH, k, p, idx, ncols, coef);
-  return cudaGetLastError() == cudaSuccess ? MFG_OK : MFG_ERR_CUDA;
+  return MFG_LAUNCH_STATUS();
 }
 
 int launch_adj_step_coef(const double *H, const double *Pi, const double *g, const double *gamma,
@@ -127,7 +127,7 @@ int launch_adj_step_coef(const double *H, const double *Pi, const double *g, con
   adj_step_coef_kernel<<<blocks(p * k, 128), 128, 0, s>>>(H, Pi, g, gamma, k, p, idx, Gamma, coefG,
                                                           bp, scal);
   adj_beta_kernel<<<blocks(p, 128), 128, 0, s>>>(scal, p, beta);
-  return cudaGetLastError() == cudaSuccess ? MFG_OK : MFG_ERR_CUDA;
+  return MFG_LAUNCH_STATUS();
 }
 
 template <typename T>
@@ -135,7 +135,7 @@ int launch_adj_lincomb(const T *U, const T *lam, const T *R, const double *scal,
                        int64_t ld, int64_t p, T *out, cudaStream_t s) {
   if (p > 65535) return MFG_ERR_UNSUPPORTED;
   adj_lincomb_kernel<T><<<dim3(blocks(n, 256), (unsigned)p), 256, 0, s>>>(U, lam, R, scal, n, ld, p, out);
-  return cudaGetLastError() == cudaSuccess ? MFG_OK : MFG_ERR_CUDA;
+  return MFG_LAUNCH_STATUS();
 }
 template int launch_adj_lincomb<float>(const float *, const float *, const float *, const double *,
                                        int64_t, int64_t, int64_t, float *, cudaStream_t);

@@ -8,6 +8,7 @@
 //   update + norm   W -= Q h2, beta = ||W||, H[j+1][j] = beta
 //   normalise       q_{j+1} = W / beta  (+ bf16 hi/lo copies for the tensor cores)
 // mirroring matfree/decomp.py:454-477 step by step, batched over the probes.
+#include <cstdio>
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -16,6 +17,15 @@
 #include "kernels.cuh"
 
 namespace mfg {
+
+static thread_local char g_last_error[512] = "";
+
+void record_error(const char *where, int line, const char *what) {
+  const char *base = where;
+  for (const char *q = where; *q; ++q)
+    if (*q == '/') base = q + 1;
+  snprintf(g_last_error, sizeof(g_last_error), "%s:%d: %s", base, line, what ? what : "");
+}
 
 // ---------------------------------------------------------------------------
 // Launch accounting: every kernel the driver issues is counted per class; when
@@ -180,7 +190,10 @@ static int apply_op(const mfg_operator *op, const T *V, int64_t ldv, T *W, int64
         src = panel;
       }
       const int rc = op->apply(op->ctx, src, W, n, p, ldw, (void *)s);
-      if (rc != 0) return MFG_ERR_CUDA;
+      if (rc != 0) {
+        record_error(__FILE__, __LINE__, "operator callback returned an error");
+        return MFG_ERR_CUDA;
+      }
       if (op->shift != 0.0) return MFG_ERR_UNSUPPORTED;  // callbacks fold their own shift
       return MFG_OK;
     }
@@ -441,7 +454,7 @@ __global__ void square_kernel(const double *x, double *y, int64_t p) {
 
 static int launch_square(const double *x, double *y, int64_t p, cudaStream_t s) {
   square_kernel<<<(unsigned)ceil_div(p, 128), 128, 0, s>>>(x, y, p);
-  return cudaGetLastError() == cudaSuccess ? MFG_OK : MFG_ERR_CUDA;
+  return MFG_LAUNCH_STATUS();
 }
 
 }  // namespace mfg
@@ -451,6 +464,8 @@ using namespace mfg;
 extern "C" {
 
 int mfg_version(void) { return 100; }
+
+const char *mfg_last_error(void) { return g_last_error; }
 
 int mfg_profile_enable(int timing) {
   Profiler &P = prof();

@@ -8,11 +8,26 @@
 
 #include "../../include/matfree_gb300.h"
 
-#define MFG_CUDA_TRY(expr)                                  \
-  do {                                                      \
-    cudaError_t _e = (expr);                                \
-    if (_e != cudaSuccess) return MFG_ERR_CUDA;             \
+namespace mfg {
+// Records the call site and CUDA error text of the most recent failure on
+// this host thread (read back through mfg_last_error()).
+void record_error(const char *where, int line, const char *what);
+inline int cuda_status(cudaError_t e, const char *where, int line) {
+  if (e == cudaSuccess) return MFG_OK;
+  record_error(where, line, cudaGetErrorString(e));
+  return MFG_ERR_CUDA;
+}
+}  // namespace mfg
+
+#define MFG_CUDA_TRY(expr)                                                  \
+  do {                                                                      \
+    const int _s = ::mfg::cuda_status((expr), __FILE__, __LINE__);          \
+    if (_s != MFG_OK) return _s;                                            \
   } while (0)
+
+// status of the kernel launch just issued (configuration errors, and sticky
+// errors of earlier kernels on the device)
+#define MFG_LAUNCH_STATUS() ::mfg::cuda_status(cudaGetLastError(), __FILE__, __LINE__)
 
 #define MFG_TRY(expr)                                       \
   do {                                                      \

@@ -323,10 +323,31 @@ static bool make_map(CUtensorMap *map, const void *base, int64_t cols, int64_t r
   cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
   cuuint32_t box[2] = {(cuuint32_t)kBK, box_rows};
   cuuint32_t estr[2] = {1, 1};
-  return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides, box,
-            estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-            kRowBytes == 128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
-            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+  const CUresult r =
+      fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides, box,
+         estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+         kRowBytes == 128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
+         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) record_error(__FILE__, __LINE__, "cuTensorMapEncodeTiled (bf16 tile) failed");
+  return r == CUDA_SUCCESS;
+}
+
+bool make_plain_tensor_map_2d(void *map128, int elem_bytes, const void *base, int64_t cols,
+                              int64_t rows, int64_t ld, uint32_t box_cols, uint32_t box_rows) {
+  auto fn = encode_fn();
+  if (!fn || (elem_bytes != 4 && elem_bytes != 8)) return false;
+  cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)ld * (cuuint64_t)elem_bytes};
+  cuuint32_t box[2] = {box_cols, box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  const CUresult r =
+      fn(reinterpret_cast<CUtensorMap *>(map128),
+         elem_bytes == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2,
+         const_cast<void *>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+         CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) record_error(__FILE__, __LINE__, "cuTensorMapEncodeTiled (basis tile) failed");
+  return r == CUDA_SUCCESS;
 }
 
 bool tcgen05_supported_shape(int64_t n, int64_t p) {
@@ -381,7 +402,7 @@ int launch_dense_tcgen05(const __nv_bfloat16 *A_hi, const __nv_bfloat16 *A_lo, i
         mahi, malo, mbhi, mblo, Vf, ldvf, W, ldw, (int)n, (int)p, BN, stages, cols, (float)shift,
         status);
   }
-  return cudaGetLastError() == cudaSuccess ? MFG_OK : MFG_ERR_CUDA;
+  return MFG_LAUNCH_STATUS();
 }
 
 }  // namespace mfg

@@ -65,6 +65,12 @@ int launch_rbf_build(const float *x, int64_t n, int dim, double s2, double ell, 
 int launch_split_bf16(const float *a, int64_t rows, int64_t cols, int64_t lda, __nv_bfloat16 *hi,
                       __nv_bfloat16 *lo, int64_t ld_out, cudaStream_t s);
 
+// dense_tcgen05.cu: 2-D tensor map without swizzle (elements of `elem_bytes`
+// = 4 or 8, `cols` contiguous, `rows` rows `ld` elements apart, box
+// box_cols x box_rows, zero fill out of bounds); false if encoding failed.
+bool make_plain_tensor_map_2d(void *map128, int elem_bytes, const void *base, int64_t cols,
+                              int64_t rows, int64_t ld, uint32_t box_cols, uint32_t box_rows);
+
 // dense_tcgen05.cu: W = A V with A in bf16 (hi, optionally lo) and the panel
 // given as bf16 hi (and lo) copies; fp32 accumulate; W fp32 + shift * Vf.
 int launch_dense_tcgen05(const __nv_bfloat16 *A_hi, const __nv_bfloat16 *A_lo, int64_t lda,

@@ -8,6 +8,10 @@
 // products in that type, and combine across threads, warps and CTAs in
 // float64; the cross-CTA sum runs in a fixed order (last-arriving CTA of a
 // probe reduces all chunk partials), so results are deterministic.
+#include <cuda.h>
+
+#include <cstdio>
+
 #include "common.cuh"
 #include "kernels.cuh"
 
@@ -81,7 +85,7 @@ int launch_sampler(int stream_id, uint32_t k0, uint32_t k1, int64_t num, int64_t
     sampler_kernel<T, 0><<<grid, kThreads, 0, s>>>(k0, k1, num, n, ld, out);
   else
     sampler_kernel<T, 1><<<grid, kThreads, 0, s>>>(k0, k1, num, n, ld, out);
-  return cudaGetLastError() == cudaSuccess ? MFG_OK : MFG_ERR_CUDA;
+  return MFG_LAUNCH_STATUS();
 }
 template int launch_sampler<float>(int, uint32_t, uint32_t, int64_t, int64_t, int64_t, float *, cudaStream_t);
 template int launch_sampler<double>(int, uint32_t, uint32_t, int64_t, int64_t, int64_t, double *, cudaStream_t);
@@ -154,7 +158,9 @@ __device__ __forceinline__ bool arrive_last(unsigned *counters, int64_t b, int n
 // ---------------------------------------------------------------------------
 
 constexpr int kColGroup = 8;  // columns reduced together (independent loads in flight)
-constexpr int kMaxProjCols = 768;  // ncols * kWarps doubles of shared memory <= 48 KB
+// ncols * kWarps doubles of dynamic shared memory must stay under the default
+// 48 KB minus the kernels' static shared memory
+constexpr int kMaxProjCols = 760;
 
 // Warp tree in the data type: one warp partial sums 32 lanes' products.
 template <typename T>
@@ -266,9 +272,13 @@ __device__ __forceinline__ bool bar_try_wait0(uint64_t *bar) {
   return ok != 0;
 }
 
+// Basis tile loads: full groups of kSPGroup vectors arrive as one 2-D tensor
+// copy (box of R rows x kSPGroup vectors, rows past n zero-filled); a tail of
+// fewer than kSPGroup vectors arrives as one 1-D bulk copy per vector.
 template <typename T, int EPT>
 __global__ void __launch_bounds__(kThreads)
-sub_proj_kernel(const T *__restrict__ Q, int64_t q_bstride, int64_t q_istride, int ncols,
+sub_proj_kernel(const __grid_constant__ CUtensorMap qmap, const T *__restrict__ Q,
+                int64_t q_bstride, int64_t q_istride, int ncols,
                 const double *__restrict__ coef, int64_t c_bstride, int64_t c_istride,
                 T *Wv, int64_t w_bstride, int64_t n, int nchunks, double *__restrict__ partials,
                 unsigned *__restrict__ counters, double *__restrict__ out, int64_t out_bstride,
@@ -299,17 +309,35 @@ sub_proj_kernel(const T *__restrict__ Q, int64_t q_bstride, int64_t q_istride, i
   __syncthreads();
   if (warp == 0) {
     // one barrier per group of columns: the update consumes columns as they
-    // land.  Lane 0 arms every barrier; the 32 lanes issue the copies.
+    // land.  Lane 0 arms every barrier and issues the 2-D tile copies of the
+    // full groups; the lanes issue the 1-D copies of the tail vectors.
+    // 2-D tensor copies need a 128-byte aligned shared destination; if the
+    // tile is not aligned, record it and load every vector with 1-D copies.
+    const bool tile_ok = (smem_addr(qs) & 127u) == 0;
+    if (!tile_ok && lane == 0 && status) atomicExch(status, (int)MFG_ERR_BAD_ARG);
+    const int full = tile_ok ? ncols / kSPGroup : 0;
+    const int kcols = (int)(q_bstride / q_istride);  // basis vectors per probe
     if (lane == 0) {
       for (int g = 0; g < ngroups; ++g) {
-        const int i1 = (g + 1) * kSPGroup < ncols ? (g + 1) * kSPGroup : ncols;
+        const bool is_full = g < full;
+        const uint32_t bytes = is_full ? (uint32_t)(kSPGroup * R * sizeof(T))
+                                       : seg_bytes * (uint32_t)(ncols - g * kSPGroup);
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
                          smem_addr(&bars[g])),
-                     "r"(seg_bytes * (uint32_t)(i1 - g * kSPGroup))
+                     "r"(bytes)
                      : "memory");
+        if (is_full) {
+          const int x = (int)r0, y = (int)(b * kcols + g * kSPGroup);
+          asm volatile(
+              "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes "
+              "[%0], [%1, {%3, %4}], [%2];" ::"r"(smem_addr(qs + (size_t)g * kSPGroup * R)),
+              "l"(reinterpret_cast<uint64_t>(&qmap)), "r"(smem_addr(&bars[g])), "r"(x), "r"(y)
+              : "memory");
+        }
       }
     }
-    for (int i = lane; i < ncols; i += 32) {
+    __syncwarp();
+    for (int i = full * kSPGroup + lane; i < ncols; i += 32) {
       const T *src = Q + b * q_bstride + (int64_t)i * q_istride + r0;
       asm volatile(
           "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
@@ -533,7 +561,7 @@ int launch_proj(const T *Q, int64_t q_bstride, int64_t q_istride, int ncols, con
   proj_kernel<T><<<grid, kThreads, smem, s>>>(Q, q_bstride, q_istride, ncols, Wv, w_bstride, n,
                                               (int)nch, partials, counters, out, out_bstride,
                                               out_istride);
-  return cudaGetLastError() == cudaSuccess ? MFG_OK : MFG_ERR_CUDA;
+  return MFG_LAUNCH_STATUS();
 }
 
 // Rows per CTA of the fused kernel: the largest of 4/2/1 rows per thread
@@ -545,12 +573,11 @@ static size_t sub_proj_smem(int ncols, int64_t R) {
          (size_t)ncols * sizeof(double);
 }
 
+// One row per thread: the 2-D tile copies load R = 256 rows per vector.
 template <typename T>
 int sub_proj_rows_per_thread(int ncols) {
   if (ncols > kMaxProjCols) return 0;
-  for (int ept = (sizeof(T) == 4 ? 4 : 2); ept >= 1; ept >>= 1)
-    if (sub_proj_smem<T>(ncols, (int64_t)kThreads * ept) <= kSubProjSmemBudget) return ept;
-  return 0;
+  return sub_proj_smem<T>(ncols, (int64_t)kThreads) <= kSubProjSmemBudget ? 1 : 0;
 }
 
 template <typename T> int64_t max_fused_chunks(int64_t n) { return ceil_div(n, kThreads); }
@@ -564,15 +591,36 @@ static int launch_sub_proj_t(const T *Q, int64_t q_bstride, int64_t q_istride, i
   const int64_t R = (int64_t)kThreads * EPT;
   const int64_t nch = ceil_div(n, R);
   const size_t smem = sub_proj_smem<T>(ncols, R);
-  if (smem > 48 * 1024)
+  if (q_istride <= 0 || q_bstride % q_istride != 0) return MFG_ERR_BAD_ARG;
+  // the basis as rows of q_istride elements: row b * k + i is probe b's vector i
+  CUtensorMap qmap;
+  const int64_t kcols = q_bstride / q_istride;
+  if (!make_plain_tensor_map_2d(&qmap, (int)sizeof(T), Q, n, p * kcols, q_istride, (uint32_t)R,
+                                (uint32_t)kSPGroup))
+    return MFG_ERR_CUDA;
+  const cudaError_t before = cudaGetLastError();
+  // The default dynamic limit is 48 KB minus the kernel's static shared
+  // memory, so the opt-in is raised well below 48 KB.
+  if (smem > 32 * 1024)
     MFG_CUDA_TRY(cudaFuncSetAttribute(sub_proj_kernel<T, EPT>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   dim3 grid((unsigned)nch, (unsigned)p);
-  sub_proj_kernel<T, EPT><<<grid, kThreads, smem, s>>>(Q, q_bstride, q_istride, ncols, coef,
+  sub_proj_kernel<T, EPT><<<grid, kThreads, smem, s>>>(qmap, Q, q_bstride, q_istride, ncols, coef,
                                                        c_bstride, c_istride, Wv, w_bstride, n,
                                                        (int)nch, partials, counters, out,
                                                        out_bstride, status);
-  return cudaGetLastError() == cudaSuccess ? MFG_OK : MFG_ERR_CUDA;
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    cudaFuncAttributes fa{};
+    cudaFuncGetAttributes(&fa, sub_proj_kernel<T, EPT>);
+    char msg[256];
+    snprintf(msg, sizeof(msg), "%s (smem %zu, maxDyn %d, static %zu, grid %ux%u, ncols %d, before %s)",
+             cudaGetErrorString(e), smem, fa.maxDynamicSharedSizeBytes, fa.sharedSizeBytes, grid.x,
+             grid.y, ncols, cudaGetErrorString(before));
+    record_error(__FILE__, __LINE__, msg);
+    return MFG_ERR_CUDA;
+  }
+  return MFG_OK;
 }
 
 template <typename T>
@@ -583,12 +631,6 @@ int launch_sub_proj(const T *Q, int64_t q_bstride, int64_t q_istride, int ncols,
   if (ncols <= 0 || p <= 0) return MFG_OK;
   if (p > 65535) return MFG_ERR_UNSUPPORTED;
   const int ept = sub_proj_rows_per_thread<T>(ncols);
-  if (ept == 4)
-    return launch_sub_proj_t<T, 4>(Q, q_bstride, q_istride, ncols, coef, c_bstride, c_istride, Wv,
-                                   w_bstride, n, p, partials, counters, out, out_bstride, status, s);
-  if (ept == 2)
-    return launch_sub_proj_t<T, 2>(Q, q_bstride, q_istride, ncols, coef, c_bstride, c_istride, Wv,
-                                   w_bstride, n, p, partials, counters, out, out_bstride, status, s);
   if (ept == 1)
     return launch_sub_proj_t<T, 1>(Q, q_bstride, q_istride, ncols, coef, c_bstride, c_istride, Wv,
                                    w_bstride, n, p, partials, counters, out, out_bstride, status, s);
@@ -606,7 +648,7 @@ int launch_sub(const T *Q, int64_t q_bstride, int64_t q_istride, int ncols, cons
   if (p > 65535) return MFG_ERR_UNSUPPORTED;
   dim3 grid((unsigned)nch, (unsigned)p);
   const size_t smem = (size_t)(ncols > 0 ? ncols : 1) * sizeof(T);
-  if (smem > 48 * 1024) return MFG_ERR_UNSUPPORTED;
+  if (smem > 40 * 1024) return MFG_ERR_UNSUPPORTED;  // under the default dynamic limit
   if (with_norm && store)
     sub_kernel<T, true, true><<<grid, kThreads, smem, s>>>(
         Q, q_bstride, q_istride, ncols, coef, c_bstride, c_istride, Win, Wout, w_bstride, n,
@@ -619,7 +661,7 @@ int launch_sub(const T *Q, int64_t q_bstride, int64_t q_istride, int ncols, cons
     sub_kernel<T, false, true><<<grid, kThreads, smem, s>>>(
         Q, q_bstride, q_istride, ncols, coef, c_bstride, c_istride, Win, Wout, w_bstride, n,
         (int)nch, partials, counters, norm_out, norm_out2, norm2_bstride);
-  return cudaGetLastError() == cudaSuccess ? MFG_OK : MFG_ERR_CUDA;
+  return MFG_LAUNCH_STATUS();
 }
 
 template <typename T>
@@ -631,13 +673,13 @@ int launch_scale(const T *Win, int64_t w_bstride, int64_t n, int64_t p, const do
   dim3 grid((unsigned)num_chunks<T>(n), (unsigned)p);
   scale_kernel<T><<<grid, kThreads, 0, s>>>(Win, w_bstride, n, norm, out, out_bstride, hi, lo,
                                             bf_bstride);
-  return cudaGetLastError() == cudaSuccess ? MFG_OK : MFG_ERR_CUDA;
+  return MFG_LAUNCH_STATUS();
 }
 
 int launch_inv(const double *x, double *y, int64_t p, cudaStream_t s) {
   if (p <= 0) return MFG_OK;
   inv_kernel<<<(unsigned)ceil_div(p, 128), 128, 0, s>>>(x, y, p);
-  return cudaGetLastError() == cudaSuccess ? MFG_OK : MFG_ERR_CUDA;
+  return MFG_LAUNCH_STATUS();
 }
 
 #define MFG_INST(T)                                                                          \

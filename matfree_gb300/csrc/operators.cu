@@ -135,7 +135,7 @@ int launch_dense_simt(const T *A, int64_t lda, const T *V, int64_t ldv, T *W, in
   if (gy > 65535) return MFG_ERR_UNSUPPORTED;
   dim3 grid((unsigned)ceil_div(n, C::BM), (unsigned)gy);
   dense_simt_kernel<T><<<grid, 256, 0, s>>>(A, lda, V, ldv, W, ldw, n, p, (T)shift);
-  return cudaGetLastError() == cudaSuccess ? MFG_OK : MFG_ERR_CUDA;
+  return MFG_LAUNCH_STATUS();
 }
 template int launch_dense_simt<float>(const float *, int64_t, const float *, int64_t, float *,
                                       int64_t, int64_t, int64_t, double, cudaStream_t);
@@ -186,7 +186,7 @@ int launch_csr_spmm(const int32_t *row_ptr, const int32_t *col_idx, const float 
   if (gy > 65535 || gx > 65535) return MFG_ERR_UNSUPPORTED;
   csr_spmm_kernel<<<dim3((unsigned)gx, (unsigned)gy), 256, 0, s>>>(row_ptr, col_idx, val, n, V,
                                                                    ldv, W, ldw, p, (float)shift);
-  return cudaGetLastError() == cudaSuccess ? MFG_OK : MFG_ERR_CUDA;
+  return MFG_LAUNCH_STATUS();
 }
 
 // ---------------------------------------------------------------------------
@@ -241,7 +241,7 @@ int launch_rbf_build(const float *x, int64_t n, int dim, double s2, double ell, 
   const double inv2l2 = 1.0 / (2.0 * ell * ell);
   rbf_kernel<<<dim3((unsigned)ceil_div(lda, 256), (unsigned)n), 256, 0, s>>>(
       x, n, dim, s2, inv2l2, precision, dlogell, a, a_lo, lda);
-  return cudaGetLastError() == cudaSuccess ? MFG_OK : MFG_ERR_CUDA;
+  return MFG_LAUNCH_STATUS();
 }
 
 __global__ void split_kernel(const float *__restrict__ a, int64_t rows, int64_t cols, int64_t lda,
@@ -262,7 +262,7 @@ int launch_split_bf16(const float *a, int64_t rows, int64_t cols, int64_t lda, _
   if (rows > 65535) return MFG_ERR_UNSUPPORTED;
   split_kernel<<<dim3((unsigned)ceil_div(ld_out, 256), (unsigned)rows), 256, 0, s>>>(
       a, rows, cols, lda, hi, lo, ld_out);
-  return cudaGetLastError() == cudaSuccess ? MFG_OK : MFG_ERR_CUDA;
+  return MFG_LAUNCH_STATUS();
 }
 
 }  // namespace mfg

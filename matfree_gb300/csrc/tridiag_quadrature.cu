@@ -65,17 +65,20 @@ __global__ void tridiag_ql_kernel(int k, int64_t p, const double *__restrict__ H
       for (int i = m - 1; i >= l; --i) {
         const double f = s * E_(i);
         const double bb = c * E_(i);
-        // entries of Lanczos tridiagonals are far from the overflow range,
-        // so the plain Euclidean norm replaces hypot; one reciprocal per rotation
-        r = sqrt(f * f + g * g);
-        E_(i + 1) = r;
-        if (r == 0.0) {  // split: recover and restart the sweep
+        // Entries of Lanczos tridiagonals are far from the overflow range, so
+        // the rotation uses one reciprocal square root of f^2 + g^2 (in place
+        // of hypot and a division): float64 issue slots are scarce on GB300.
+        const double rr = fma(f, f, g * g);
+        if (rr == 0.0) {  // split: recover and restart the sweep
+          E_(i + 1) = 0.0;
           D_(i + 1) -= shift_acc;
           E_(m) = 0.0;
           deflated = true;
           break;
         }
-        const double rinv = 1.0 / r;
+        const double rinv = rsqrt(rr);
+        r = rr * rinv;
+        E_(i + 1) = r;
         s = f * rinv;
         c = g * rinv;
         g = D_(i + 1) - shift_acc;
@@ -137,7 +140,7 @@ int launch_tridiag_quadrature(int64_t k, int64_t p, const double *H, int32_t fun
                               double *first_sq, int *status, cudaStream_t s) {
   if (p <= 0 || k <= 0) return MFG_OK;
   const size_t per_thread = (size_t)3 * k * sizeof(double);
-  const size_t budget = 48 * 1024;
+  const size_t budget = 46 * 1024;  // under the default dynamic shared-memory limit
   if (per_thread > budget) return MFG_ERR_UNSUPPORTED;
   // The solve is a serial float64 chain per problem: spread the problems over
   // all SMs (a few threads per CTA) so that no SM's float64 pipe is shared
@@ -152,7 +155,7 @@ int launch_tridiag_quadrature(int64_t k, int64_t p, const double *H, int32_t fun
   const unsigned grid = (unsigned)ceil_div(p, tb);
   tridiag_ql_kernel<<<grid, tb, (size_t)tb * per_thread, s>>>((int)k, p, H, fun, param, scale,
                                                               values, eigvals, first_sq, status);
-  return cudaGetLastError() == cudaSuccess ? MFG_OK : MFG_ERR_CUDA;
+  return MFG_LAUNCH_STATUS();
 }
 
 // mean and standard error (population std / sqrt(p)) of p values; one CTA.
@@ -191,7 +194,7 @@ __global__ void mean_sem_kernel(const double *__restrict__ v, int64_t p, double 
 int launch_mean_sem(const double *values, int64_t p, double *mean_sem, cudaStream_t s) {
   if (p <= 0) return MFG_ERR_BAD_ARG;
   mean_sem_kernel<<<1, kThreads, 0, s>>>(values, p, mean_sem);
-  return cudaGetLastError() == cudaSuccess ? MFG_OK : MFG_ERR_CUDA;
+  return MFG_LAUNCH_STATUS();
 }
 
 }  // namespace mfg

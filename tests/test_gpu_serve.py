@@ -1,0 +1,63 @@
+"""The continuous-batching server: alone == in the mix, admission, parity."""
+
+import numpy as np
+import pytest
+
+from matfree_gb300 import serve
+from oracle import philox, problems, slq
+
+pytestmark = pytest.mark.gpu
+
+
+def _requests(num=6, seed=3):
+    reqs = serve.synthetic_stream(num, rate=1e6, seed=seed, n_range=(512, 2048), ks=(16, 24),
+                                  ps=(32, 64))
+    for r in reqs:
+        r.arrival = 0.0
+    return reqs
+
+
+def test_result_is_identical_alone_and_in_the_mix():
+    reqs = _requests()
+    alone = []
+    for r in reqs:
+        res, _ = serve.SLQServer(slots=1).run([r], realtime=False)
+        alone.append(res[0])
+    mixed, stats = serve.SLQServer(slots=4).run(reqs, realtime=False)
+    assert stats["solves"] == len(reqs)
+    for a, m in zip(alone, mixed):
+        assert a.rid == m.rid
+        assert a.mean == m.mean and a.sem == m.sem  # bit-identical: deterministic kernels
+
+
+def test_admission_respects_the_memory_budget():
+    reqs = _requests(num=5, seed=4)
+    biggest = max(serve.footprint_bytes(r.x.shape[0], r.k, r.p, "bf16x3") for r in reqs)
+    server = serve.SLQServer(slots=4, budget_bytes=1.5 * biggest)
+    seen = []
+    orig = server._launch
+
+    def spy(slot, req):
+        seen.append(server.used)
+        return orig(slot, req)
+
+    server._launch = spy
+    res, stats = server.run(reqs, realtime=False)
+    assert stats["solves"] == len(reqs)
+    assert max(seen) <= 1.5 * biggest
+    with pytest.raises(ValueError, match="budget"):
+        serve.SLQServer(slots=1, budget_bytes=biggest / 10).run(reqs[:1], realtime=False)
+
+
+@pytest.mark.parametrize("fun", ["log", "exp:-0.1"])
+def test_served_value_matches_oracle(fun):
+    n, k, p = 1024, 24, 32
+    x = problems.rbf_points(n, seed=9).astype(np.float32)
+    req = serve.Request(rid=0, x=x, k=k, p=p, fun=fun, key=(7, 0))
+    (res,), _ = serve.SLQServer(slots=1).run([req], realtime=False)
+    K = problems.rbf_kernel(x.astype(np.float64))
+    V = philox.rademacher(np.array([7, 0], dtype=np.uint32), p, n)
+    f = np.log if fun == "log" else (lambda t: np.exp(-0.1 * t))
+    want = slq.slq_batched(lambda X: X @ K, k, V, matfun=f)
+    assert abs(res.mean - want.mean()) <= 1e-4 * abs(want.mean())
+    np.testing.assert_allclose(res.sem, want.std() / np.sqrt(p), rtol=1e-3)
