@@ -42,7 +42,8 @@ enum {
   MFG_ERR_CUDA = 4,        /* a CUDA runtime/driver call failed               */
   MFG_ERR_UNSUPPORTED = 5, /* combination not implemented (e.g. op/precision) */
   MFG_ERR_NO_CONVERGENCE = 6, /* tridiagonal eigensolver hit its sweep limit  */
-  MFG_ERR_TIMEOUT = 7      /* a bounded device-side wait gave up             */
+  MFG_ERR_TIMEOUT = 7,     /* a bounded device-side wait gave up             */
+  MFG_ERR_SCRATCH_LIMIT = 8 /* problem larger than a fixed static scratch     */
 };
 
 /* ---- element type of vectors and bases --------------------------------- */
@@ -215,6 +216,27 @@ MFG_API int mfg_profile_read(int32_t nclasses, double *ms, double *bytes, double
 
 MFG_API int mfg_split_bf16(const float *a, int64_t rows, int64_t cols, int64_t lda,
                    void *hi, void *lo, int64_t ld_out, void *stream);
+
+/* Operator application that allocates nothing: the same W = (A + shift I) V
+ * as mfg_operator_apply, for callers that cannot allocate device memory
+ * (code running inside another framework's memory pool, an allocator-free
+ * embedded host, or a CUDA stream capture where allocation is not allowed)
+ * and therefore cannot provide a workspace.  It has no counterpart in the
+ * reference (matfree is JAX and never manages device memory itself).
+ *
+ * The only scratch it needs, the bf16 hi/lo copies of the probe panel for
+ * the tensor-core precisions, lives in one fixed array inside this library:
+ * MFG_NOALLOC_SCRATCH_BYTES (32 MiB) of device memory that every GPU which
+ * loads the library holds until the process exits.  Panels needing more
+ * (p * ld * 4 bytes > 32 MiB for bf16x3, p * ld * 2 bytes for bf16) are
+ * rejected with MFG_ERR_SCRATCH_LIMIT before any work is queued.  The first
+ * call on a device looks up that device's copy of the array (no allocation);
+ * make that first call before any stream capture.  All calls share the one
+ * array: calls that overlap on the GPU (other streams, other threads) race
+ * on it and must be serialised by the caller. */
+#define MFG_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
+MFG_API int mfg_operator_apply_noalloc(const mfg_operator *op, const void *V, void *W,
+                                       int64_t p, int64_t ld, void *stream);
 
 #ifdef __cplusplus
 }

@@ -20,6 +20,7 @@ MFG_ERR_CUDA = 4
 MFG_ERR_UNSUPPORTED = 5
 MFG_ERR_NO_CONVERGENCE = 6
 MFG_ERR_TIMEOUT = 7
+MFG_ERR_SCRATCH_LIMIT = 8
 
 MFG_F32, MFG_F64 = 0, 1
 MFG_OP_DENSE, MFG_OP_CSR, MFG_OP_CALLBACK = 0, 1, 2
@@ -66,6 +67,7 @@ SIGNATURES = {
     "mfg_split_bf16": (c_int, [c_void_p, c_int64, c_int64, c_int64, c_void_p, c_void_p, c_int64, c_void_p]),
     "mfg_adjoint_workspace_bytes": (c_size_t, [POINTER(MfgOperator), c_int64, c_int64, c_int64]),
     "mfg_hessenberg_adjoint": (c_int, [POINTER(MfgOperator), c_int64, c_int64, c_int64, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
+    "mfg_operator_apply_noalloc":(c_int, [POINTER(MfgOperator), c_void_p, c_void_p, c_int64, c_int64, c_void_p]),
     "mfg_profile_enable": (c_int, [c_int]),
     "mfg_profile_read": (c_int, [c_int32, POINTER(c_double), POINTER(c_double), POINTER(c_double), POINTER(c_int64)]),
 }

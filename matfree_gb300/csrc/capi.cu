@@ -509,6 +509,8 @@ const char *mfg_status_string(int status) {
     case MFG_ERR_UNSUPPORTED: return "unsupported operator/precision/shape";
     case MFG_ERR_NO_CONVERGENCE: return "tridiagonal eigensolver did not converge";
     case MFG_ERR_TIMEOUT: return "a bounded device-side wait timed out";
+    case MFG_ERR_SCRATCH_LIMIT:
+      return "problem exceeds the fixed 32 MiB scratch of the no-allocation entry point";
     default: return "unknown status";
   }
 }
@@ -574,6 +576,70 @@ int mfg_operator_apply(const mfg_operator *op, const void *V, void *W, int64_t p
   }
   return apply_op<float>(op, (const float *)V, ld, (float *)W, ld, p, hi, lo, ld,
                          reinterpret_cast<float *>(ws + L.panel), status, s);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Operator application without any allocation.
+//
+// The panel's bf16 copies go to a file-scope device array instead of a
+// caller workspace.  In host code `g_noalloc_scratch` names a host-side shadow,
+// not device memory, so its device address is looked up per device with
+// cudaGetSymbolAddress (with that device current) on the first call there
+// and cached.  Layout: [0, 256) status word, then hi, then lo.
+// ---------------------------------------------------------------------------
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[MFG_NOALLOC_SCRATCH_BYTES];
+
+namespace mfg {
+constexpr int kMaxDevices = 64;
+static std::mutex g_noalloc_mu;
+static void *g_noalloc_ptr[kMaxDevices] = {nullptr};
+
+static int noalloc_scratch(void **out) {
+  int dev = 0;
+  MFG_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) return MFG_ERR_UNSUPPORTED;
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void *ptr = nullptr;
+    if (cudaGetSymbolAddress(&ptr, g_noalloc_scratch) != cudaSuccess || ptr == nullptr)
+      return MFG_ERR_CUDA;
+    g_noalloc_ptr[dev] = ptr;
+  }
+  *out = g_noalloc_ptr[dev];
+  return MFG_OK;
+}
+}  // namespace mfg
+
+extern "C" {
+
+int mfg_operator_apply_noalloc(const mfg_operator *op, const void *V, void *W, int64_t p,
+                               int64_t ld, void *stream) {
+  MFG_TRY(check_op(op));
+  MFG_TRY(check_panel(op, p, ld));
+  if (!V || !W || !aligned16(V) || !aligned16(W)) return MFG_ERR_BAD_ARG;
+  // scratch need: status word + bf16 hi (+ lo) copies of the panel
+  const size_t copies = uses_bf16(op) ? (op->precision == MFG_PREC_BF16X3 ? 2 : 1) : 0;
+  const size_t panel_bytes = align_up((size_t)p * (size_t)ld * 2, 256);
+  if (256 + copies * panel_bytes > MFG_NOALLOC_SCRATCH_BYTES) return MFG_ERR_SCRATCH_LIMIT;
+  void *base = nullptr;
+  MFG_TRY(noalloc_scratch(&base));
+  char *sc = reinterpret_cast<char *>(base);
+  cudaStream_t s = as_stream(stream);
+  int *status = reinterpret_cast<int *>(sc);
+  MFG_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int), s));
+  if (op->precision == MFG_PREC_FP64)
+    return apply_op<double>(op, (const double *)V, ld, (double *)W, ld, p, nullptr, nullptr, ld,
+                            nullptr, status, s);
+  __nv_bfloat16 *hi = nullptr, *lo = nullptr;
+  if (copies > 0) {
+    hi = reinterpret_cast<__nv_bfloat16 *>(sc + 256);
+    lo = copies == 2 ? reinterpret_cast<__nv_bfloat16 *>(sc + 256 + panel_bytes) : nullptr;
+    MFG_TRY(launch_split_bf16((const float *)V, p, op->n, ld, hi, lo, ld, s));
+  }
+  return apply_op<float>(op, (const float *)V, ld, (float *)W, ld, p, hi, lo, ld, nullptr, status, s);
 }
 
 int mfg_hessenberg(const mfg_operator *op, int64_t k, int64_t p, const void *V, int64_t ld,
