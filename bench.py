@@ -38,6 +38,8 @@ CONFIGS = {
     # small case of the same kernels for ncu captures (operator 268 MB and
     # basis 134 MB: both above L2)
     "rbf8k": ("rbf", 8192, 16, 256),
+    # same, with the bench depth k = 64 (basis 537 MB) for captures of late steps
+    "rbf8k64": ("rbf", 8192, 64, 256),
     "dense1k": ("dense", 1000, 30, 100),
     "laplace1m": ("csr", 1024 * 1024, 100, 64),
 }
@@ -167,7 +169,22 @@ def build_problem(cfg, seed=0):
     return {"kind": kind, "n": n, "k": k, "p": p, "csr": A}
 
 
+class _Slot:
+    """One in-flight solve: its stream, workspace and result buffers."""
+
+    def __init__(self, torch, dev):
+        from matfree_gb300._panel import Workspace
+
+        self.stream = torch.cuda.Stream(device=dev)
+        self.ws = Workspace()
+        self.mean_sem = torch.zeros(2, dtype=torch.float64, device=dev)
+        self.host = torch.zeros(2, dtype=torch.float64).pin_memory()
+        self.done = torch.cuda.Event()
+
+
 def gpu_arm(args):
+    import ctypes
+
     import torch
 
     import matfree_gb300 as mf
@@ -180,7 +197,6 @@ def gpu_arm(args):
     precision = args.precision
     dev = torch.device("cuda", torch.cuda.current_device())
     key = mf.prng.prng_key(1 + rank)
-    mean_sem = torch.zeros(2, dtype=torch.float64, device=dev)
 
     if kind == "rbf":
         x_host = torch.from_numpy(prob["x"]).pin_memory()
@@ -193,23 +209,43 @@ def gpu_arm(args):
         static = mf.CSROperator.from_scipy(prob["csr"], device=dev)
         x_host = x_dev = None
     sampler = mf.stochtrace.sampler_signs(torch.ones(n, device=dev), num=p)
+    slots = [_Slot(torch, dev) for _ in range(max(1, args.inflight))]
 
-    def solve(x):
-        if kind == "rbf":
-            op = mf.RBFKernelOperator(x, s2=prob["s2"], ell=prob["ell"], tau=prob["tau"], precision=precision)
-        else:
-            op = static
-        V = sampler(key)
-        return slq_values(op, k, V, _lib.MFG_FUN_LOG, 0.0, mean_sem=mean_sem)
+    def solve(x, slot, h2d=False):
+        """One complete solve enqueued on the slot's stream."""
+        with torch.cuda.stream(slot.stream):
+            if h2d:
+                x = x_host.to(dev, non_blocking=True)
+            if kind == "rbf":
+                op = mf.RBFKernelOperator(x, s2=prob["s2"], ell=prob["ell"], tau=prob["tau"],
+                                          precision=precision)
+            else:
+                op = static
+            V = sampler(key)
+            vals = slq_values(op, k, V, _lib.MFG_FUN_LOG, 0.0, mean_sem=slot.mean_sem,
+                              workspace=slot.ws)
+            if h2d:
+                slot.host.copy_(slot.mean_sem, non_blocking=True)
+            slot.done.record(slot.stream)
+        return vals
 
-    # warm-up
-    for _ in range(args.warmup):
-        solve(x_dev)
+    def join_all():
+        cur = torch.cuda.current_stream()
+        for s in slots:
+            cur.wait_stream(s.stream)
+
+    def fork_all():
+        for s in slots:
+            s.stream.wait_stream(torch.cuda.current_stream())
+
+    for i in range(args.warmup):
+        solve(x_dev, slots[i % len(slots)])
+    join_all()
     torch.cuda.synchronize()
-
-    # timed region: device-resident inputs, per-step events, launch accounting
     lib = _lib.lib()
-    lib.mfg_profile_enable(1)
+
+    # (1) throughput: solves round-robin over the in-flight slots, device-resident inputs
+    lib.mfg_profile_enable(0)  # launch counting only
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     _barrier(world)
@@ -218,10 +254,13 @@ def gpu_arm(args):
         t0 = torch.cuda.Event(enable_timing=True)
         t1 = torch.cuda.Event(enable_timing=True)
         t0.record()
+        fork_all()
         for i in range(args.steps):
-            starts[i].record()
-            values = solve(x_dev)
-            ends[i].record()
+            slot = slots[i % len(slots)]
+            starts[i].record(slot.stream)
+            values = solve(x_dev, slot)
+            ends[i].record(slot.stream)
+        join_all()
         t1.record()
         torch.cuda.synchronize()
         _barrier(world)
@@ -229,32 +268,48 @@ def gpu_arm(args):
     total_ms = _max_over_ranks(t0.elapsed_time(t1), world)
     step_ms = sorted(s.elapsed_time(e) for s, e in zip(starts, ends))
     nc = len(_lib.PROF_CLASSES)
-    ms = (ctypes_arr := __import__("ctypes").c_double * nc)()
-    by = ctypes_arr()
-    fl = ctypes_arr()
-    ln = (__import__("ctypes").c_int64 * nc)()
-    _lib.check(lib.mfg_profile_read(nc, ms, by, fl, ln), "mfg_profile_read")
-    lib.mfg_profile_enable(0)
-    prof = {c: {"ms": ms[i], "bytes": by[i], "flops": fl[i], "launches": int(ln[i])}
-            for i, c in enumerate(_lib.PROF_CLASSES)}
-    est = float(mean_sem[0].item())
+    ln = (ctypes.c_int64 * nc)()
+    _lib.check(lib.mfg_profile_read(nc, None, None, None, ln), "mfg_profile_read")
+    launches = int(sum(ln))
+    est = float(slots[(args.steps - 1) % len(slots)].mean_sem[0].item())
 
-    # end to end through the public API: host points in, scalar out
+    # (2) roofline: the same steps on one stream, every launch bracketed by events
+    lib.mfg_profile_enable(1)
+    torch.cuda.synchronize()
+    for i in range(args.steps):
+        solve(x_dev, slots[0])
+    torch.cuda.synchronize()
+    ms = (ctypes.c_double * nc)()
+    by = (ctypes.c_double * nc)()
+    fl = (ctypes.c_double * nc)()
+    ln1 = (ctypes.c_int64 * nc)()
+    _lib.check(lib.mfg_profile_read(nc, ms, by, fl, ln1), "mfg_profile_read")
+    lib.mfg_profile_enable(0)
+    prof = {c: {"ms": ms[i], "bytes": by[i], "flops": fl[i], "launches": int(ln1[i])}
+            for i, c in enumerate(_lib.PROF_CLASSES)}
+
+    # (3) end to end through the public API: pinned host points in, (mean, sem) out
     e2e = None
     if kind == "rbf":
         torch.cuda.synchronize()
         _barrier(world)
         t_start = time.perf_counter()
-        for _ in range(args.steps):
-            xd = x_host.to(dev, non_blocking=True)
-            solve(xd)
-            _ = float(mean_sem[0].item())
+        for i in range(args.steps):
+            slot = slots[i % len(slots)]
+            if i >= len(slots):
+                slot.done.synchronize()
+                _ = float(slot.host[0])  # the result of the solve this slot ran before
+            solve(None, slot, h2d=True)
+        for i in range(max(0, args.steps - len(slots)), args.steps):
+            slots[i % len(slots)].done.synchronize()
+            _ = float(slots[i % len(slots)].host[0])
         e2e_s = _max_over_ranks(time.perf_counter() - t_start, world)
         e2e = {"value": world * args.steps / e2e_s, "unit": UNIT,
-               "h2d_bytes_per_step": int(x_host.numel() * 4), "d2h_bytes_per_step": 8}
+               "h2d_bytes_per_step": int(x_host.numel() * 4), "d2h_bytes_per_step": 16}
 
     result = {"rank": rank, "world": world, "total_ms": total_ms, "step_ms": step_ms, "prof": prof,
-              "clocks": clocks, "estimate": est, "e2e": e2e, "values": values, "key": key}
+              "clocks": clocks, "estimate": est, "e2e": e2e, "values": values, "key": key,
+              "launches": launches}
     return result, prob
 
 
@@ -446,7 +501,7 @@ def serve_arm(args):
     clocks = clk.summary()
     plain = serve.SLQServer(slots=1, budget_bytes=150e9, precision="fp32")
     plain.run(warm[:1], realtime=False)
-    base_reqs = reqs[: args.baseline_requests]
+    base_reqs = reqs[: args.baseline_requests] if args.baseline_requests > 0 else reqs
     _, bstats = plain.run(base_reqs, realtime=False)
     work = sum(2.0 * r.x.shape[0] ** 2 * r.p * r.k * 3 for r in reqs)
     line = {"metric": METRIC, "value": stats["solves_per_s"], "unit": UNIT, "n_gpus": 1,
@@ -473,9 +528,12 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="rbf16k", choices=sorted(CONFIGS) + ["serve", "grad8k"])
     ap.add_argument("--requests", type=int, default=64)
-    ap.add_argument("--baseline-requests", type=int, default=24)
+    ap.add_argument("--baseline-requests", type=int, default=0,
+                    help="requests of the plain fp32 comparison (0: all of them)")
     ap.add_argument("--rate", type=float, default=150.0)
     ap.add_argument("--slots", type=int, default=8)
+    ap.add_argument("--inflight", type=int, default=2,
+                    help="independent solves in flight (round-robin over CUDA streams)")
     ap.add_argument("--precision", default="bf16x3", choices=["fp32", "bf16", "bf16x3", "fp64"])
     ap.add_argument("--cpu-probes", type=int, default=8)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -503,7 +561,7 @@ def main():
     value = world * args.steps / (res["total_ms"] / 1e3)
     rl = roofline(res["prof"], peaks, args.steps)
     rl["peak_source"] = f"of {peaks['source']}"
-    launches = sum(v["launches"] for v in res["prof"].values())
+    launches = res["launches"]
     step_ms = res["step_ms"]
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

@@ -126,7 +126,10 @@ MFG_API int mfg_operator_apply(const mfg_operator *op, const void *V, void *W, i
  * Q (p*k rows of ld), H (p k x k float64), residual (p rows of ld) and
  * init_len_inv[p] = 1/||v_b||.
  * Replaces decomp.tridiag_sym(k, reortho="full") / decomp.hessenberg
- * (matfree/decomp.py:30-152, 353-477).  reortho: 1 = "full", 0 = "none". */
+ * (matfree/decomp.py:30-152, 353-477).  reortho: 1 = "full" (Gram-Schmidt
+ * twice against all vectors), 0 = "none" of hessenberg (once against all
+ * vectors), 2 = three-term Lanczos of tridiag_sym(reortho="none")
+ * (decomp.py:215-291: H holds a_j on the diagonal and b_j below it). */
 MFG_API int mfg_hessenberg(const mfg_operator *op, int64_t k, int64_t p, const void *V,
                    int64_t ld, int32_t reortho, void *Q, double *H, void *residual,
                    double *init_len_inv, void *workspace, size_t workspace_bytes,

@@ -273,6 +273,26 @@ static int run_hessenberg(const mfg_operator *op, int64_t k, int64_t p, const T 
     const int ncols = (int)(j + 1);
     const double pb = (ncols + 1.0) * vecb, pf = 2.0 * ncols * vecb / sizeof(T);
     const double ub = (ncols + 2.0) * vecb;
+    if (reortho == 2) {
+      // three-term Lanczos (matfree/decomp.py:215-291): a_j = q_j^T A q_j into
+      // H[j][j]; w -= b_{j-1} q_{j-1} + a_j q_j with both coefficients read from
+      // row j of H (H[j][j-1] = b_{j-1}, H[j][j] = a_j); b_j = ||w|| into H[j+1][j]
+      const bool last3 = (j + 1 == k);
+      MFG_LAUNCH(MFG_PROF_PROJ, 2.0 * vecb, 2.0 * vecb / sizeof(T),
+                 launch_proj<T>(qj, qb, ld, 1, Wb, ld, n, p, partials, counters, H + j * k + j,
+                                k * k, 1, s));
+      const int nc = j == 0 ? 1 : 2;
+      const T *qbase = Q + (j == 0 ? 0 : (j - 1) * ld);
+      const double *cf = H + j * k + (j == 0 ? 0 : j - 1);
+      MFG_LAUNCH(MFG_PROF_SUB, (nc + 2.0) * vecb, 2.0 * nc * vecb / sizeof(T),
+                 launch_sub<T>(qbase, qb, ld, nc, cf, k * k, 1, Wb, Wb, ld, n, p, true, true,
+                               partials, counters, norm, last3 ? nullptr : H + (j + 1) * k + j, k * k,
+                               s));
+      if (!last3)
+        MFG_LAUNCH(MFG_PROF_SCALE, 2.0 * vecb + bfb, vecb / sizeof(T),
+                   launch_scale<T>(Wb, ld, n, p, norm, Q + (j + 1) * ld, qb, hi, lo, ld, s));
+      continue;
+    }
     // first pass: h = Q^T w into column j of H
     MFG_LAUNCH(MFG_PROF_PROJ, pb, pf,
                launch_proj<T>(Q, qb, ld, ncols, Wb, ld, n, p, partials, counters, H + j, k * k, k, s));
@@ -650,7 +670,7 @@ int mfg_hessenberg(const mfg_operator *op, int64_t k, int64_t p, const void *V, 
   if (k < 0 || k > op->n) return MFG_ERR_RANGE;
   if (!V || !aligned16(V) || (k > 0 && (!Q || !H || !aligned16(Q)))) return MFG_ERR_BAD_ARG;
   if (residual && !aligned16(residual)) return MFG_ERR_BAD_ARG;
-  if (reortho != 0 && reortho != 1) return MFG_ERR_BAD_ARG;
+  if (reortho < 0 || reortho > 2) return MFG_ERR_BAD_ARG;
   const WsLayout L = layout(op, k, p, ld);
   if (!workspace || workspace_bytes < L.total) return MFG_ERR_WORKSPACE;
   char *ws = ws_base(workspace);

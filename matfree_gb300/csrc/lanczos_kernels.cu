@@ -160,7 +160,7 @@ __device__ __forceinline__ bool arrive_last(unsigned *counters, int64_t b, int n
 constexpr int kColGroup = 8;  // columns reduced together (independent loads in flight)
 // ncols * kWarps doubles of dynamic shared memory must stay under the default
 // 48 KB minus the kernels' static shared memory
-constexpr int kMaxProjCols = 760;
+constexpr int kMaxProjCols = 640;  // 40 KB dynamic + ~2.2 KB static
 
 // Warp tree in the data type: one warp partial sums 32 lanes' products.
 template <typename T>
@@ -186,10 +186,29 @@ __device__ __forceinline__ void finish_columns(const double *red, int ncols, int
   }
   if (nchunks == 1) return;
   if (arrive_last(counters, b, nchunks)) {
-    for (int i = threadIdx.x; i < ncols; i += kThreads) {
+    // G threads per column sum strided chunk partials, then a fixed-order
+    // tree over those G sums: the last CTA's reduction is parallel and the
+    // result does not depend on timing.
+    __shared__ double s_red[kThreads];
+    int G = 1;
+    while (G < 32 && 2 * G * ncols <= kThreads && G < nchunks) G *= 2;
+    const int cols_per_pass = kThreads / G;
+    const int g = threadIdx.x % G;
+    for (int i0 = 0; i0 < ncols; i0 += cols_per_pass) {
+      const int i = i0 + (int)threadIdx.x / G;
       double t = 0.0;
-      for (int cc = 0; cc < nchunks; ++cc) t += __ldcg(&partials[(b * nchunks + cc) * ncols + i]);
-      out[b * out_bstride + i * out_istride] = t;
+      if (i < ncols) {
+#pragma unroll 4
+        for (int cc = g; cc < nchunks; cc += G) t += __ldcg(&partials[(b * nchunks + cc) * ncols + i]);
+      }
+      s_red[threadIdx.x] = t;
+      __syncthreads();
+      for (int st = G / 2; st > 0; st >>= 1) {
+        if (g < st) s_red[threadIdx.x] += s_red[threadIdx.x + st];
+        __syncthreads();
+      }
+      if (g == 0 && i < ncols) out[b * out_bstride + i * out_istride] = s_red[threadIdx.x];
+      __syncthreads();
     }
     if (threadIdx.x == 0) counters[b] = 0u;
   }
@@ -483,10 +502,19 @@ sub_kernel(const T *__restrict__ Q, int64_t q_bstride, int64_t q_istride, int nc
   }
   if (nchunks == 1) return;
   if (arrive_last(counters, b, nchunks)) {
+    // strided per-thread sums, then a fixed-order tree (deterministic)
+    __shared__ double s_red[kThreads];
+    double t = 0.0;
+#pragma unroll 4
+    for (int cc = threadIdx.x; cc < nchunks; cc += kThreads) t += __ldcg(&partials[b * nchunks + cc]);
+    s_red[threadIdx.x] = t;
+    __syncthreads();
+    for (int st = kThreads / 2; st > 0; st >>= 1) {
+      if ((int)threadIdx.x < st) s_red[threadIdx.x] += s_red[threadIdx.x + st];
+      __syncthreads();
+    }
     if (threadIdx.x == 0) {
-      double t = 0.0;
-      for (int cc = 0; cc < nchunks; ++cc) t += __ldcg(&partials[b * nchunks + cc]);
-      const double nv = sqrt(t);
+      const double nv = sqrt(s_red[0]);
       norm_out[b] = nv;
       if (norm_out2) norm_out2[b * norm2_bstride] = nv;
       counters[b] = 0u;

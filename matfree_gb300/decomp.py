@@ -62,8 +62,8 @@ def run_hessenberg(op, k: int, V: torch.Tensor, *, reortho: str = "full", worksp
     lib = _lib.lib()
     nbytes = lib.mfg_slq_workspace_bytes(ctypes.byref(s), k, p, ld)
     ws, wsb = (workspace or _WS).get(nbytes, V.device)
-    st = lib.mfg_hessenberg(ctypes.byref(s), k, p, ctypes.c_void_p(panel.data_ptr()), ld,
-                            1 if reortho == "full" else 0,
+    mode = {"none": 0, "full": 1, "lanczos": 2}[reortho]
+    st = lib.mfg_hessenberg(ctypes.byref(s), k, p, ctypes.c_void_p(panel.data_ptr()), ld, mode,
                             ctypes.c_void_p(Q.data_ptr() if k > 0 else 0),
                             ctypes.c_void_p(H.data_ptr() if k > 0 else 0),
                             ctypes.c_void_p(R.data_ptr()), ctypes.c_void_p(c.data_ptr()),
@@ -125,6 +125,24 @@ class _TridiagSymFull(_Decomposition):
         return _DecompResult(Q_tall=Q, J_small=J, residual=r, init_length_inv=c.to(out_dt))
 
 
+class _TridiagSymNone(_Decomposition):
+    """Three-term Lanczos without reorthogonalisation (matfree/decomp.py:155-291)."""
+
+    reortho = "none"
+
+    def batched(self, matvec, V: torch.Tensor, *params) -> _DecompResult:
+        op = as_operator(matvec, V.shape[1], V.dtype, params)
+        k = self.num_matvecs
+        # k = 0 still applies the operator once for the residual (decomp.py:230-237)
+        Q, H, r, c = run_hessenberg(op, max(k, 1), V, reortho="lanczos")
+        Q, H = Q[:, :k], H[:, :k, :k]
+        out_dt = V.dtype if V.dtype in (torch.float32, torch.float64) else torch.float32
+        d = torch.diagonal(H, 0, -2, -1).to(out_dt)
+        e = torch.diagonal(H, -1, -2, -1).to(out_dt)
+        J = _todense_tridiag_sym(d, e) if self.materialize else (d, e)
+        return _DecompResult(Q_tall=Q, J_small=J, residual=r, init_length_inv=c.to(out_dt))
+
+
 class _Hessenberg(_Decomposition):
     def __init__(self, num_matvecs, *, reortho, custom_vjp, reortho_vjp):
         super().__init__(num_matvecs, materialize=True, custom_vjp=custom_vjp)
@@ -157,10 +175,7 @@ def tridiag_sym(num_matvecs: int, /, *, materialize: bool = True, reortho: str =
     if reortho == "full":
         return _TridiagSymFull(num_matvecs, materialize=materialize, custom_vjp=custom_vjp)
     if reortho == "none":
-        raise NotImplementedError(
-            "tridiag_sym(reortho='none') (three-term Lanczos without reorthogonalisation) is not "
-            "provided by matfree_gb300; use reortho='full'."
-        )
+        return _TridiagSymNone(num_matvecs, materialize=materialize, custom_vjp=custom_vjp)
     msg = f"reortho={reortho} unsupported. Choose eiter {'full', 'none'}."
     raise ValueError(msg)
 

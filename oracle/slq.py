@@ -73,6 +73,45 @@ def tridiag_sym_full(matvec, num_matvecs, v, *, materialize=True):
     return Q.T.copy(), J, r, c
 
 
+def tridiag_sym_none(matvec, num_matvecs, vec, *, materialize=True):
+    """matfree/decomp.py:155-212 and 215-291: three-term Lanczos, no reorthogonalisation.
+
+    v0 = vec/||vec||; a = v.Av; r = Av - a v - b v_prev; b = ||r||; x = r/b.
+    Returns (Q_tall (k, n), T or (diag, offdiag), residual = b x, 1/||vec||).
+    """
+    vec = np.asarray(vec, dtype=np.float64)
+    n = vec.shape[0]
+    k = num_matvecs
+    if k < 0 or k > n:
+        raise ValueError(error_num_matvecs(k, maxval=n, minval=0))
+    vectors = np.zeros((k + 1, n))
+    diags = np.zeros(k)
+    offdiags = np.zeros(k)
+    v0 = vec / np.linalg.norm(vec)
+    vectors[0] = v0
+    Av = matvec(v0)
+    a = v0 @ Av
+    r = Av - a * v0
+    b = np.linalg.norm(r)
+    x = r / b
+    if k == 0:
+        Q, d, e = vectors[:-1], diags, offdiags[:-1]
+    else:
+        vectors[1], offdiags[0], diags[0] = x, b, a
+        v1, v_prev = x, v0
+        for i in range(1, k):
+            Av = matvec(v1)
+            a = v1 @ Av
+            r = Av - a * v1 - b * v_prev
+            b = np.linalg.norm(r)
+            x = r / b
+            vectors[i + 1], offdiags[i], diags[i] = x, b, a
+            v1, v_prev = x, v1
+        Q, d, e = vectors[:-1], diags, offdiags[:-1]
+    J = todense_tridiag_sym(d, e) if materialize else (d, e)
+    return Q, J, b * x, 1.0 / np.linalg.norm(vec)
+
+
 def todense_tridiag_sym(diag, off_diag):
     """matfree/decomp.py:148-152."""
     return np.diag(diag) + np.diag(off_diag, -1) + np.diag(off_diag, 1)
