@@ -261,167 +261,14 @@ proj_kernel(const T *__restrict__ Q, int64_t q_bstride, int64_t q_istride, int n
   finish_columns(red, ncols, b, c, nchunks, partials, counters, out, out_bstride, out_istride);
 }
 
-// ---------------------------------------------------------------------------
-// Fused second pass: w' = w - Q c, then h2 = Q^T w' from one read of Q.
-//
-// The CTA owns R = kThreads * EPT consecutive rows of one probe.  One thread
-// issues a bulk asynchronous copy per basis vector (its R-row segment) into
-// shared memory, all completing on one mbarrier; the CTA then forms w' from
-// shared memory, stores it, and reads the same shared tile again for the
-// projections.  This removes one of the four basis sweeps of a CGS2 step.
-// ---------------------------------------------------------------------------
-
+// Shared-memory address and bulk-copy constants of the fused second pass
+// (streamed kernel below).
 __device__ __forceinline__ uint32_t smem_addr(const void *p) {
   return (uint32_t)__cvta_generic_to_shared(p);
 }
 
 constexpr uint32_t kBarWaitLimit = 1u << 24;
-constexpr int kSPGroup = 8;                                    // columns per copy barrier
-constexpr int kMaxSPGroups = (kMaxProjCols + kSPGroup - 1) / kSPGroup;
-constexpr size_t kSubProjSmemBudget = 110 * 1024;              // two CTAs per SM
-
-__device__ __forceinline__ bool bar_try_wait0(uint64_t *bar) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}\n"
-      : "=r"(ok)
-      : "r"(smem_addr(bar))
-      : "memory");
-  return ok != 0;
-}
-
-// Basis tile loads: full groups of kSPGroup vectors arrive as one 2-D tensor
-// copy (box of R rows x kSPGroup vectors, rows past n zero-filled); a tail of
-// fewer than kSPGroup vectors arrives as one 1-D bulk copy per vector.
-template <typename T, int EPT>
-__global__ void __launch_bounds__(kThreads)
-sub_proj_kernel(const __grid_constant__ CUtensorMap qmap, const T *__restrict__ Q,
-                int64_t q_bstride, int64_t q_istride, int ncols,
-                const double *__restrict__ coef, int64_t c_bstride, int64_t c_istride,
-                T *Wv, int64_t w_bstride, int64_t n, int nchunks, double *__restrict__ partials,
-                unsigned *__restrict__ counters, double *__restrict__ out, int64_t out_bstride,
-                int *__restrict__ status) {
-  constexpr int R = kThreads * EPT;
-  extern __shared__ __align__(128) uint8_t smem[];
-  T *qs = reinterpret_cast<T *>(smem);                       // [ncols][R]
-  T *ws = qs + (size_t)ncols * R;                            // [R]  w' of this chunk
-  T *s_coef = ws + R;                                        // [ncols]
-  double *red = reinterpret_cast<double *>(s_coef + ((ncols + 1) & ~1));  // [ncols]
-  __shared__ __align__(8) uint64_t bars[kMaxSPGroups];
-  __shared__ int s_fail;
-
-  const int64_t c = blockIdx.x;
-  const int64_t b = blockIdx.y;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int64_t r0 = c * R;
-  const int64_t rows = (n - r0 < R) ? (n - r0) : R;
-  const uint32_t seg_bytes = (uint32_t)(((rows * (int64_t)sizeof(T)) + 15) / 16 * 16);
-  const int ngroups = (ncols + kSPGroup - 1) / kSPGroup;
-
-  if (threadIdx.x == 0) {
-    for (int g = 0; g < ngroups; ++g)
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bars[g])) : "memory");
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    s_fail = 0;
-  }
-  __syncthreads();
-  if (warp == 0) {
-    // one barrier per group of columns: the update consumes columns as they
-    // land.  Lane 0 arms every barrier and issues the 2-D tile copies of the
-    // full groups; the lanes issue the 1-D copies of the tail vectors.
-    // 2-D tensor copies need a 128-byte aligned shared destination; if the
-    // tile is not aligned, record it and load every vector with 1-D copies.
-    const bool tile_ok = (smem_addr(qs) & 127u) == 0;
-    if (!tile_ok && lane == 0 && status) atomicExch(status, (int)MFG_ERR_BAD_ARG);
-    const int full = tile_ok ? ncols / kSPGroup : 0;
-    const int kcols = (int)(q_bstride / q_istride);  // basis vectors per probe
-    if (lane == 0) {
-      for (int g = 0; g < ngroups; ++g) {
-        const bool is_full = g < full;
-        const uint32_t bytes = is_full ? (uint32_t)(kSPGroup * R * sizeof(T))
-                                       : seg_bytes * (uint32_t)(ncols - g * kSPGroup);
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
-                         smem_addr(&bars[g])),
-                     "r"(bytes)
-                     : "memory");
-        if (is_full) {
-          const int x = (int)r0, y = (int)(b * kcols + g * kSPGroup);
-          asm volatile(
-              "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes "
-              "[%0], [%1, {%3, %4}], [%2];" ::"r"(smem_addr(qs + (size_t)g * kSPGroup * R)),
-              "l"(reinterpret_cast<uint64_t>(&qmap)), "r"(smem_addr(&bars[g])), "r"(x), "r"(y)
-              : "memory");
-        }
-      }
-    }
-    __syncwarp();
-    for (int i = full * kSPGroup + lane; i < ncols; i += 32) {
-      const T *src = Q + b * q_bstride + (int64_t)i * q_istride + r0;
-      asm volatile(
-          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-          ::"r"(smem_addr(qs + (size_t)i * R)), "l"(reinterpret_cast<uint64_t>(src)),
-          "r"(seg_bytes), "r"(smem_addr(&bars[i / kSPGroup]))
-          : "memory");
-    }
-  }
-  for (int i = threadIdx.x; i < ncols; i += kThreads) s_coef[i] = (T)coef[b * c_bstride + i * c_istride];
-
-  // this thread's EPT consecutive rows
-  const int64_t rt = r0 + (int64_t)threadIdx.x * EPT;
-  T w[EPT];
-#pragma unroll
-  for (int e = 0; e < EPT; ++e) w[e] = (rt + e < n) ? Wv[b * w_bstride + rt + e] : (T)0;
-  __syncthreads();
-
-  const T *qrow = qs + (size_t)threadIdx.x * EPT;
-  volatile int *fail = &s_fail;
-  for (int g = 0; g < ngroups; ++g) {
-    // bounded wait for this group's basis segments
-    bool ready = false;
-    for (uint32_t it = 0; it < kBarWaitLimit; ++it) {
-      if (bar_try_wait0(&bars[g])) {
-        ready = true;
-        break;
-      }
-      if ((it & 1023u) == 1023u && *fail) break;
-    }
-    if (!ready) {
-      *fail = 1;
-      if (status) atomicExch(status, (int)MFG_ERR_TIMEOUT);
-      break;
-    }
-    const int i1 = (g + 1) * kSPGroup < ncols ? (g + 1) * kSPGroup : ncols;
-    for (int i = g * kSPGroup; i < i1; ++i) {
-      const T ci = s_coef[i];
-#pragma unroll
-      for (int e = 0; e < EPT; ++e) w[e] = fma(-qrow[(size_t)i * R + e], ci, w[e]);
-    }
-  }
-  __syncthreads();
-  if (s_fail) return;
-#pragma unroll
-  for (int e = 0; e < EPT; ++e) {
-    if (rt + e < n) Wv[b * w_bstride + rt + e] = w[e];
-    ws[threadIdx.x * EPT + e] = (rt + e < n) ? w[e] : (T)0;
-  }
-  __syncthreads();
-
-  // h2: warp `warp` owns columns warp, warp + 8, ...; its lanes stride the
-  // R rows of the chunk, so one warp reduction covers R products.  Rows past
-  // n hold stale shared memory and are left out.
-  for (int i = warp; i < ncols; i += kWarps) {
-    const T *col = qs + (size_t)i * R;
-    T acc = (T)0;
-#pragma unroll 4
-    for (int r = lane; r < R; r += 32)
-      if (r < rows) acc = fma(col[r], ws[r], acc);
-    acc = warp_sum_t<T>(acc);
-    if (lane == 0) red[i] = (double)acc;
-  }
-  __syncthreads();
-  finish_columns(red, ncols, b, c, nchunks, partials, counters, out, out_bstride, 1, 1);
-}
+constexpr int kSPGroup = 8;  // basis vectors per 2-D tensor copy
 
 // ---------------------------------------------------------------------------
 // Update w -= Q c, optionally with ||w|| (float64) fused
@@ -592,63 +439,437 @@ int launch_proj(const T *Q, int64_t q_bstride, int64_t q_istride, int ncols, con
   return MFG_LAUNCH_STATUS();
 }
 
-// Rows per CTA of the fused kernel: the largest of 4/2/1 rows per thread
-// (width-limited for doubles) whose basis tile fits the shared-memory budget.
-// shared memory of the fused kernel: basis tile, w' tile, coefficients, column sums
-template <typename T>
-static size_t sub_proj_smem(int ncols, int64_t R) {
-  return (size_t)ncols * R * sizeof(T) + (size_t)R * sizeof(T) + (size_t)(ncols + 2) * sizeof(T) +
-         (size_t)ncols * sizeof(double);
+// ---------------------------------------------------------------------------
+// Fused second pass of CGS2: w' = w - Q h1 and h2 = Q^T w' from one read of
+// the basis (streamed, row-owner form).
+//
+// The p * C row chunks of 128 rows (probe b, chunk c -> flat index b C + c)
+// are cut into one equal contiguous range per resident CTA, so every SM
+// streams the same share.  A CTA walks its range through a ring of nbuf
+// shared-memory buffers filled by a copy warp: 2-D tensor copies of 128 rows
+// x 8 basis vectors, 1-D copies for a tail of fewer than 8 vectors and for
+// the chunk's rows of w, all completing on the buffer's "full" barrier; the
+// four row warps release a buffer through its "empty" barrier.  Thread j
+// owns row j of every chunk:
+//   w'[j] = w[j] - sum_i q_i[j] c_i           (its own row only)
+//   h2_i += q_i[j] w'[j]   for every i        (a register per vector)
+// so no data crosses threads until the CTA leaves a probe, when the
+// per-thread float sums (one product per chunk) go through a warp butterfly
+// and a fixed-order float64 sum over warps.  A probe split between CTAs is
+// finished by the last of them to arrive, summing their partials in CTA
+// order, so results do not depend on timing.  Vectors are padded to a
+// multiple of 8 with zero columns that no copy writes.
+// ---------------------------------------------------------------------------
+
+// Bounded wait for the phase of `bar` with the given parity; every 1024
+// polls it gives up early if `fail` (when given) is set.
+__device__ __forceinline__ bool bar_wait_bounded(uint64_t *bar, uint32_t parity,
+                                                 volatile int *fail,
+                                                 uint32_t limit = kBarWaitLimit) {
+  for (uint32_t it = 0; it < limit; ++it) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    if (fail && (it & 1023u) == 1023u && *fail) return false;
+  }
+  return false;
 }
 
-// One row per thread: the 2-D tile copies load R = 256 rows per vector.
-template <typename T>
-int sub_proj_rows_per_thread(int ncols) {
-  if (ncols > kMaxProjCols) return 0;
-  return sub_proj_smem<T>(ncols, (int64_t)kThreads) <= kSubProjSmemBudget ? 1 : 0;
+constexpr int kSThreads = 128;
+constexpr int kSWarps = kSThreads / 32;
+constexpr int kSR = 128;
+constexpr int kSMaxBuf = 8;
+constexpr int kSMaxGroups = 16;  // ncols <= 128
+
+// Per-thread sums of N values -> per-warp sums: a halving butterfly (each
+// step a lane keeps half of its values and adds its partner's copy of that
+// half), so N values cost N - N/32 shuffles instead of 5 N.  Afterwards lane
+// `lane` holds in v[i], i < max(N / 32, 1), the warp sum of value
+// xsum_index<N>(lane, i); for N < 32 lanes with the same index hold copies.
+template <int N>
+__device__ __forceinline__ int xsum_index(int lane, int i) {
+  int idx = i;
+#pragma unroll
+  for (int s = 0; s < 5; ++s)
+    if ((N >> (s + 1)) >= 1 && (lane & (16 >> s))) idx += N >> (s + 1);
+  return idx;
 }
 
-template <typename T> int64_t max_fused_chunks(int64_t n) { return ceil_div(n, kThreads); }
+template <typename T, int N>
+__device__ __forceinline__ void warp_xsum(T (&v)[N], int lane) {
+#pragma unroll
+  for (int s = 0; s < 5; ++s) {
+    const int o = 16 >> s;
+    const int half = N >> (s + 1);
+    if (half >= 1) {
+      const bool up = (lane & o) != 0;
+#pragma unroll
+      for (int i = 0; i < half; ++i) {
+        const T send = up ? v[i] : v[i + half];
+        const T keep = up ? v[i + half] : v[i];
+        v[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+      }
+    } else {
+      v[0] += __shfl_xor_sync(0xffffffffu, v[0], o);
+    }
+  }
+}
 
-template <typename T, int EPT>
-static int launch_sub_proj_t(const T *Q, int64_t q_bstride, int64_t q_istride, int ncols,
-                             const double *coef, int64_t c_bstride, int64_t c_istride, T *Wv,
-                             int64_t w_bstride, int64_t n, int64_t p, double *partials,
-                             unsigned *counters, double *out, int64_t out_bstride, int *status,
-                             cudaStream_t s) {
-  const int64_t R = (int64_t)kThreads * EPT;
-  const int64_t nch = ceil_div(n, R);
-  const size_t smem = sub_proj_smem<T>(ncols, R);
+__device__ __forceinline__ void row_warps_sync() {
+  asm volatile("bar.sync 1, %0;" ::"n"(kSThreads) : "memory");
+}
+
+// The flat chunk sequence f = b * C + c (probe b, chunk c of C) is cut into
+// gridDim.x equal ranges; range x is [F x / G, F (x + 1) / G).  The CTA that
+// covers flat chunk f:
+__device__ __forceinline__ int64_t cta_of_chunk(int64_t f, int64_t F, int64_t G) {
+  return ((f + 1) * G - 1) / F;
+}
+
+template <typename T, int MAXG, bool kHold>
+__global__ void __launch_bounds__(kSThreads + 32)
+sub_proj_stream_kernel(const __grid_constant__ CUtensorMap qmap, const T *__restrict__ Q,
+                       int64_t q_bstride, int64_t q_istride, int ncols,
+                       const double *__restrict__ coef, int64_t c_bstride, int64_t c_istride,
+                       T *Wv, int64_t w_bstride, int64_t n, int64_t p, int nbuf, int pstride,
+                       double *__restrict__ partials, unsigned *__restrict__ counters,
+                       double *__restrict__ out, int64_t out_bstride, int *__restrict__ status) {
+  extern __shared__ __align__(128) uint8_t smem[];
+  const int ngroups = (ncols + kSPGroup - 1) / kSPGroup;
+  const int cpad = ngroups * kSPGroup;
+  // ring of nbuf buffers [cpad + 1][kSR]: the chunk's basis rows (zero
+  // columns past ncols), then its rows of w
+  T *bufs = reinterpret_cast<T *>(smem);
+  const size_t bstr = (size_t)(cpad + 1) * kSR;
+  T *s_coef = bufs + nbuf * bstr;  // [cpad], zero past ncols
+  __shared__ __align__(8) uint64_t full_bar[kSMaxBuf];   // copies of the chunk landed
+  __shared__ __align__(8) uint64_t empty_bar[kSMaxBuf];  // every row warp is done with it
+  __shared__ double red[kSWarps][kSPGroup * kSMaxGroups];
+  __shared__ int s_fail;
+  __shared__ int s_last;
+
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t C = (n + kSR - 1) / kSR;
+  const int64_t F = p * C;
+  const int64_t G = gridDim.x;
+  const int64_t f_begin = F * (int64_t)blockIdx.x / G;
+  const int64_t f_end = F * ((int64_t)blockIdx.x + 1) / G;
+  const int kcols = (int)(q_bstride / q_istride);
+
+  if (threadIdx.x == 0) {
+    for (int u = 0; u < nbuf; ++u) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&full_bar[u])) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(&empty_bar[u])),
+                   "r"(kSWarps)
+                   : "memory");
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    s_fail = 0;
+  }
+  if (threadIdx.x < kSR)
+    for (int u = 0; u < nbuf; ++u)
+      for (int i = ncols; i < cpad; ++i) bufs[u * bstr + (size_t)i * kSR + threadIdx.x] = (T)0;
+  // 2-D tensor copies need a 128-byte aligned shared destination; if the
+  // ring is not aligned, record it and load every vector with 1-D copies
+  const bool tile_ok = (smem_addr(bufs) & 127u) == 0;
+  if (!tile_ok && threadIdx.x == 0 && status) atomicExch(status, (int)MFG_ERR_BAD_ARG);
+  const int full = tile_ok ? ncols / kSPGroup : 0;
+  __syncthreads();
+  volatile int *fail = &s_fail;
+
+  if (warp == kSWarps) {
+    // copy warp: chunk t of this CTA goes into buffer t % nbuf once the row
+    // warps have released that buffer's previous chunk; lane c issues
+    // copies c, c + 32, ...
+    int issued = 0;
+    const int ncopies = full + (ncols - full * kSPGroup) + 1;
+    for (int64_t f = f_begin; f < f_end; ++f) {
+      const int t = (int)(f - f_begin);
+      const int u = t % nbuf;
+      if (t >= nbuf && !bar_wait_bounded(&empty_bar[u], (uint32_t)((t / nbuf - 1) & 1), fail)) {
+        if (lane == 0) {
+          *fail = 1;
+          if (status) atomicExch(status, (int)MFG_ERR_TIMEOUT);
+        }
+        break;
+      }
+      const int64_t b = f / C;
+      const int64_t r0 = (f - b * C) * kSR;
+      const int64_t rows = (n - r0 < kSR) ? (n - r0) : kSR;
+      const uint32_t seg_bytes = (uint32_t)(((rows * (int64_t)sizeof(T)) + 15) / 16 * 16);
+      const uint32_t bytes = (uint32_t)full * (uint32_t)(kSPGroup * kSR * sizeof(T)) +
+                             seg_bytes * (uint32_t)(ncols - full * kSPGroup + 1);
+      if (lane == 0)
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
+                         smem_addr(&full_bar[u])),
+                     "r"(bytes)
+                     : "memory");
+      __syncwarp();
+      T *dst = bufs + u * bstr;
+      for (int c = lane; c < ncopies; c += 32) {
+        if (c < full) {
+          const int x = (int)r0, y = (int)(b * kcols + c * kSPGroup);
+          asm volatile(
+              "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes "
+              "[%0], [%1, {%3, %4}], [%2];" ::"r"(smem_addr(dst + (size_t)c * kSPGroup * kSR)),
+              "l"(reinterpret_cast<uint64_t>(&qmap)), "r"(smem_addr(&full_bar[u])), "r"(x), "r"(y)
+              : "memory");
+        } else {
+          // a tail vector, or (last copy) the chunk's rows of w
+          const int i = full * kSPGroup + (c - full);
+          const bool is_w = c == ncopies - 1;
+          const T *src = is_w ? Wv + b * w_bstride + r0 : Q + b * q_bstride + (int64_t)i * q_istride + r0;
+          T *d = dst + (size_t)(is_w ? cpad : i) * kSR;
+          asm volatile(
+              "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+              ::"r"(smem_addr(d)), "l"(reinterpret_cast<uint64_t>(src)), "r"(seg_bytes),
+              "r"(smem_addr(&full_bar[u]))
+              : "memory");
+        }
+      }
+      issued = t + 1;
+    }
+    if (*fail && lane == 0) {
+      // the copies of the last chunks issued land (bounded) before the CTA's
+      // shared memory goes away; earlier buffers were consumed before reuse
+      for (int t = (issued > nbuf ? issued - nbuf : 0); t < issued; ++t)
+        bar_wait_bounded(&full_bar[t % nbuf], (uint32_t)((t / nbuf) & 1), nullptr, kBarWaitLimit >> 4);
+    }
+  } else {
+    // row warps: thread j owns row j of every chunk
+    const int j = threadIdx.x;
+    T acc[kSPGroup * MAXG];
+#pragma unroll
+    for (int i = 0; i < kSPGroup * MAXG; ++i) acc[i] = (T)0;
+    int64_t b = -1;
+    for (int64_t f = f_begin; f < f_end; ++f) {
+      const int t = (int)(f - f_begin);
+      const int u = t % nbuf;
+      if (b != f / C) {
+        // a new probe: its coefficients (the row warps are past every read
+        // of the previous ones)
+        row_warps_sync();
+        b = f / C;
+        for (int i = j; i < cpad; i += kSThreads)
+          s_coef[i] = i < ncols ? (T)coef[b * c_bstride + i * c_istride] : (T)0;
+        row_warps_sync();
+      }
+      // After a failure every row warp still walks the remaining chunks
+      // (without waiting or computing), so all of them meet at the same
+      // named barriers.
+      bool ready = false;
+      if (!*fail) {
+        ready = bar_wait_bounded(&full_bar[u], (uint32_t)((t / nbuf) & 1), fail);
+        if (!ready) {
+          *fail = 1;
+          if (status) atomicExch(status, (int)MFG_ERR_TIMEOUT);
+        }
+      }
+      const T *buf = bufs + u * bstr + j;  // this thread's row, column stride kSR
+      const int64_t r0 = (f - b * C) * kSR;
+      const int rows = (int)((n - r0 < kSR) ? (n - r0) : kSR);
+      // w' = w - Q c over this thread's row; four interleaved sums shorten
+      // the dependent chain
+      T qv[kHold ? kSPGroup * MAXG : 1];
+      T w0 = ready ? buf[(size_t)cpad * kSR] : (T)0, w1 = (T)0, w2 = (T)0, w3 = (T)0;
+#pragma unroll
+      for (int g = 0; g < MAXG; ++g)
+        if (ready && g < ngroups) {
+#pragma unroll
+          for (int e = 0; e < kSPGroup; e += 4) {
+            const int i = g * kSPGroup + e;
+            const T q0 = buf[(size_t)i * kSR], q1 = buf[(size_t)(i + 1) * kSR];
+            const T q2 = buf[(size_t)(i + 2) * kSR], q3 = buf[(size_t)(i + 3) * kSR];
+            if constexpr (kHold) {
+              qv[i] = q0;
+              qv[i + 1] = q1;
+              qv[i + 2] = q2;
+              qv[i + 3] = q3;
+            }
+            w0 = fma(-q0, s_coef[i], w0);
+            w1 = fma(-q1, s_coef[i + 1], w1);
+            w2 = fma(-q2, s_coef[i + 2], w2);
+            w3 = fma(-q3, s_coef[i + 3], w3);
+          }
+        }
+      const T w = (w0 + w1) + (w2 + w3);
+      // rows past the probe's end hold stale shared memory and are left out
+      if (ready && j < rows) {
+        Wv[b * w_bstride + r0 + j] = w;
+#pragma unroll
+        for (int g = 0; g < MAXG; ++g)
+          if (g < ngroups) {
+#pragma unroll
+            for (int e = 0; e < kSPGroup; ++e) {
+              const int i = g * kSPGroup + e;
+              const T q = kHold ? qv[kHold ? i : 0] : buf[(size_t)i * kSR];
+              acc[i] = fma(q, w, acc[i]);
+            }
+          }
+      }
+      __syncwarp();
+      if (lane == 0 && ready)
+        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(&empty_bar[u])) : "memory");
+
+      // the probe's last row chunk in this CTA: its share of h2
+      if (f + 1 == f_end || (f + 1) / C != b) {
+        warp_xsum<T, kSPGroup * MAXG>(acc, lane);
+        constexpr int kPer = (kSPGroup * MAXG) / 32 > 0 ? (kSPGroup * MAXG) / 32 : 1;
+        constexpr int kDup = (kSPGroup * MAXG) >= 32 ? 1 : 32 / (kSPGroup * MAXG);
+        if ((lane & (kDup - 1)) == 0) {
+#pragma unroll
+          for (int i = 0; i < kPer; ++i) red[warp][xsum_index<kSPGroup * MAXG>(lane, i)] = (double)acc[i];
+        }
+#pragma unroll
+        for (int i = 0; i < kSPGroup * MAXG; ++i) acc[i] = (T)0;
+        row_warps_sync();
+        double h = 0.0;
+        if (j < ncols) {
+#pragma unroll
+          for (int q = 0; q < kSWarps; ++q) h += red[q][j];
+        }
+        const int64_t first = cta_of_chunk(b * C, F, G), last = cta_of_chunk(b * C + C - 1, F, G);
+        if (first == last) {
+          if (j < ncols) out[b * out_bstride + j] = h;
+        } else {
+          const int64_t seg = (int64_t)blockIdx.x - first;
+          if (j < ncols) partials[(b * pstride + seg) * ncols + j] = h;
+          __threadfence();
+          row_warps_sync();
+          if (j == 0) {
+            const unsigned ticket = atomicAdd(&counters[b], 1u);
+            s_last = ticket == (unsigned)(last - first);
+          }
+          row_warps_sync();
+          if (s_last) {
+            __threadfence();
+            if (j < ncols) {
+              double v = 0.0;
+              for (int64_t q = 0; q <= last - first; ++q)
+                v += __ldcg(&partials[(b * pstride + q) * ncols + j]);
+              out[b * out_bstride + j] = v;
+            }
+            if (j == 0) counters[b] = 0u;
+          }
+        }
+        // red and s_last are reused at this CTA's next probe
+        row_warps_sync();
+      }
+    }
+  }
+  __syncthreads();
+}
+
+template <typename T>
+static size_t sub_proj_stream_smem(int ncols, int nbuf) {
+  const int cpad = (ncols + kSPGroup - 1) / kSPGroup * kSPGroup;
+  return (size_t)nbuf * (cpad + 1) * kSR * sizeof(T) + (size_t)cpad * sizeof(T);
+}
+
+// Largest vector count of the streamed kernel: 128 floats, 64 doubles (the
+// per-thread sums live in registers).
+template <typename T> constexpr int sub_proj_stream_max_cols() { return sizeof(T) == 4 ? 128 : 64; }
+
+// Ring depth: as many buffers (2..8) as fit in ~110 KB, so that two CTAs
+// share an SM; 0 if even two do not fit in ~220 KB.
+template <typename T>
+static int sub_proj_stream_buffers(int ncols) {
+  if (ncols < 1 || ncols > sub_proj_stream_max_cols<T>()) return 0;
+  int nb = kSMaxBuf;
+  while (nb > 2 && sub_proj_stream_smem<T>(ncols, nb) > 110 * 1024) --nb;
+  return sub_proj_stream_smem<T>(ncols, nb) <= 220 * 1024 ? nb : 0;
+}
+
+template <typename T, int MAXG, bool kHold>
+static int launch_sub_proj_stream_t(const T *Q, int64_t q_bstride, int64_t q_istride, int ncols,
+                                    const double *coef, int64_t c_bstride, int64_t c_istride,
+                                    T *Wv, int64_t w_bstride, int64_t n, int64_t p,
+                                    double *partials, unsigned *counters, double *out,
+                                    int64_t out_bstride, int *status, cudaStream_t s) {
+  const int nbuf = sub_proj_stream_buffers<T>(ncols);
+  if (nbuf < 2) return MFG_ERR_UNSUPPORTED;
+  const size_t smem = sub_proj_stream_smem<T>(ncols, nbuf);
   if (q_istride <= 0 || q_bstride % q_istride != 0) return MFG_ERR_BAD_ARG;
-  // the basis as rows of q_istride elements: row b * k + i is probe b's vector i
-  CUtensorMap qmap;
-  const int64_t kcols = q_bstride / q_istride;
-  if (!make_plain_tensor_map_2d(&qmap, (int)sizeof(T), Q, n, p * kcols, q_istride, (uint32_t)R,
-                                (uint32_t)kSPGroup))
-    return MFG_ERR_CUDA;
-  const cudaError_t before = cudaGetLastError();
+  auto kern = sub_proj_stream_kernel<T, MAXG, kHold>;
   // The default dynamic limit is 48 KB minus the kernel's static shared
   // memory, so the opt-in is raised well below 48 KB.
   if (smem > 32 * 1024)
-    MFG_CUDA_TRY(cudaFuncSetAttribute(sub_proj_kernel<T, EPT>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  dim3 grid((unsigned)nch, (unsigned)p);
-  sub_proj_kernel<T, EPT><<<grid, kThreads, smem, s>>>(qmap, Q, q_bstride, q_istride, ncols, coef,
-                                                       c_bstride, c_istride, Wv, w_bstride, n,
-                                                       (int)nch, partials, counters, out,
-                                                       out_bstride, status);
-  const cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) {
-    cudaFuncAttributes fa{};
-    cudaFuncGetAttributes(&fa, sub_proj_kernel<T, EPT>);
-    char msg[256];
-    snprintf(msg, sizeof(msg), "%s (smem %zu, maxDyn %d, static %zu, grid %ux%u, ncols %d, before %s)",
-             cudaGetErrorString(e), smem, fa.maxDynamicSharedSizeBytes, fa.sharedSizeBytes, grid.x,
-             grid.y, ncols, cudaGetErrorString(before));
-    record_error(__FILE__, __LINE__, msg);
-    return MFG_ERR_CUDA;
+    MFG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  // resident CTAs per SM for this vector count (cached: the answer depends
+  // only on the shared-memory size, i.e. on ncols)
+  static int per_sm_cache[129];
+  static int sms = 0;
+  if (sms == 0) {
+    int dev = 0;
+    MFG_CUDA_TRY(cudaGetDevice(&dev));
+    MFG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   }
-  return MFG_OK;
+  int per_sm = per_sm_cache[ncols];
+  if (per_sm == 0) {
+    MFG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kSThreads + 32, smem));
+    if (per_sm < 1) return MFG_ERR_UNSUPPORTED;
+    per_sm_cache[ncols] = per_sm;
+  }
+  // One wave of CTAs, each with an equal share of the p * C row chunks.  A
+  // probe then spans at most ceil(G / p) + 1 CTAs, whose partial sums must
+  // fit the workspace's max_fused_chunks(n) slots per probe.
+  const int64_t C = ceil_div(n, kSR);
+  const int64_t F = p * C;
+  const int64_t cap = max_fused_chunks<T>(n);
+  int64_t G = (int64_t)sms * per_sm;
+  if (G > F) G = F;
+  if (G > p * (cap - 1)) G = p * (cap - 1);
+  if (G < 1) G = 1;
+  const int pstride = (int)(ceil_div(G, p) + 1);
+  // the basis as rows of q_istride elements: row b * k + i is probe b's vector i
+  CUtensorMap qmap;
+  const int64_t kcols = q_bstride / q_istride;
+  if (!make_plain_tensor_map_2d(&qmap, (int)sizeof(T), Q, n, p * kcols, q_istride, (uint32_t)kSR,
+                                (uint32_t)kSPGroup))
+    return MFG_ERR_CUDA;
+  kern<<<(unsigned)G, kSThreads + 32, smem, s>>>(qmap, Q, q_bstride, q_istride, ncols, coef,
+                                                 c_bstride, c_istride, Wv, w_bstride, n, p, nbuf,
+                                                 pstride, partials, counters, out, out_bstride,
+                                                 status);
+  return MFG_LAUNCH_STATUS();
+}
+
+template <typename T>
+static int launch_sub_proj_stream(const T *Q, int64_t q_bstride, int64_t q_istride, int ncols,
+                                  const double *coef, int64_t c_bstride, int64_t c_istride, T *Wv,
+                                  int64_t w_bstride, int64_t n, int64_t p, double *partials,
+                                  unsigned *counters, double *out, int64_t out_bstride, int *status,
+                                  cudaStream_t s) {
+  // register sums sized to the vector count (8, 32, 64 or 128 of them); up
+  // to 64 the basis values also stay in registers between the two passes
+#define MFG_SPS(G, H)                                                                            \
+  return launch_sub_proj_stream_t<T, G, H>(Q, q_bstride, q_istride, ncols, coef, c_bstride,     \
+                                           c_istride, Wv, w_bstride, n, p, partials, counters,  \
+                                           out, out_bstride, status, s)
+  if (ncols <= 8) MFG_SPS(1, true);
+  if (ncols <= 32) MFG_SPS(4, true);
+  if (ncols <= 64) MFG_SPS(8, sizeof(T) == 4);
+  if constexpr (sizeof(T) == 4) MFG_SPS(16, false);
+#undef MFG_SPS
+  return MFG_ERR_UNSUPPORTED;
+}
+
+// 1 when the fused update+projection applies to this vector count, else 0.
+template <typename T>
+int sub_proj_rows_per_thread(int ncols) {
+  return sub_proj_stream_buffers<T>(ncols) > 0 ? 1 : 0;
+}
+
+// Partial-sum slots per probe of the cross-CTA reductions (at least 2: the
+// streamed update+projection splits a probe between up to ceil(G / p) + 1 CTAs).
+template <typename T> int64_t max_fused_chunks(int64_t n) {
+  const int64_t c = ceil_div(n, kThreads);
+  return c < 2 ? 2 : c;
 }
 
 template <typename T>
@@ -657,12 +878,9 @@ int launch_sub_proj(const T *Q, int64_t q_bstride, int64_t q_istride, int ncols,
                     int64_t p, double *partials, unsigned *counters, double *out,
                     int64_t out_bstride, int *status, cudaStream_t s) {
   if (ncols <= 0 || p <= 0) return MFG_OK;
-  if (p > 65535) return MFG_ERR_UNSUPPORTED;
-  const int ept = sub_proj_rows_per_thread<T>(ncols);
-  if (ept == 1)
-    return launch_sub_proj_t<T, 1>(Q, q_bstride, q_istride, ncols, coef, c_bstride, c_istride, Wv,
+  if (sub_proj_stream_buffers<T>(ncols) == 0) return MFG_ERR_UNSUPPORTED;
+  return launch_sub_proj_stream<T>(Q, q_bstride, q_istride, ncols, coef, c_bstride, c_istride, Wv,
                                    w_bstride, n, p, partials, counters, out, out_bstride, status, s);
-  return MFG_ERR_UNSUPPORTED;
 }
 
 template <typename T>
