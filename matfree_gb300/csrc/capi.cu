@@ -280,14 +280,14 @@ static int run_hessenberg(const mfg_operator *op, int64_t k, int64_t p, const T 
       const bool last3 = (j + 1 == k);
       MFG_LAUNCH(MFG_PROF_PROJ, 2.0 * vecb, 2.0 * vecb / sizeof(T),
                  launch_proj<T>(qj, qb, ld, 1, Wb, ld, n, p, partials, counters, H + j * k + j,
-                                k * k, 1, s));
+                                k * k, 1, s, status));
       const int nc = j == 0 ? 1 : 2;
       const T *qbase = Q + (j == 0 ? 0 : (j - 1) * ld);
       const double *cf = H + j * k + (j == 0 ? 0 : j - 1);
       MFG_LAUNCH(MFG_PROF_SUB, (nc + 2.0) * vecb, 2.0 * nc * vecb / sizeof(T),
                  launch_sub<T>(qbase, qb, ld, nc, cf, k * k, 1, Wb, Wb, ld, n, p, true, true,
                                partials, counters, norm, last3 ? nullptr : H + (j + 1) * k + j, k * k,
-                               s));
+                               s, status));
       if (!last3)
         MFG_LAUNCH(MFG_PROF_SCALE, 2.0 * vecb + bfb, vecb / sizeof(T),
                    launch_scale<T>(Wb, ld, n, p, norm, Q + (j + 1) * ld, qb, hi, lo, ld, s));
@@ -295,7 +295,7 @@ static int run_hessenberg(const mfg_operator *op, int64_t k, int64_t p, const T 
     }
     // first pass: h = Q^T w into column j of H
     MFG_LAUNCH(MFG_PROF_PROJ, pb, pf,
-               launch_proj<T>(Q, qb, ld, ncols, Wb, ld, n, p, partials, counters, H + j, k * k, k, s));
+               launch_proj<T>(Q, qb, ld, ncols, Wb, ld, n, p, partials, counters, H + j, k * k, k, s, status));
     const bool last = (j + 1 == k);
     double *hsub = last ? nullptr : H + (j + 1) * k + j;
     if (reortho && sub_proj_rows_per_thread<T>(ncols) > 0) {
@@ -305,20 +305,20 @@ static int run_hessenberg(const mfg_operator *op, int64_t k, int64_t p, const T 
                                     counters, h2, k, status, s));
       MFG_LAUNCH(MFG_PROF_SUB, ub, pf + 2.0 * vecb / sizeof(T),
                  launch_sub<T>(Q, qb, ld, ncols, h2, k, 1, Wb, Wb, ld, n, p, true, true, partials,
-                               counters, norm, hsub, k * k, s));
+                               counters, norm, hsub, k * k, s, status));
     } else if (reortho) {
       MFG_LAUNCH(MFG_PROF_SUB, ub, pf,
                  launch_sub<T>(Q, qb, ld, ncols, H + j, k * k, k, Wb, Wb, ld, n, p, false, true,
-                               partials, counters, norm, nullptr, 0, s));
+                               partials, counters, norm, nullptr, 0, s, status));
       MFG_LAUNCH(MFG_PROF_PROJ, pb, pf,
-                 launch_proj<T>(Q, qb, ld, ncols, Wb, ld, n, p, partials, counters, h2, k, 1, s));
+                 launch_proj<T>(Q, qb, ld, ncols, Wb, ld, n, p, partials, counters, h2, k, 1, s, status));
       MFG_LAUNCH(MFG_PROF_SUB, ub, pf + 2.0 * vecb / sizeof(T),
                  launch_sub<T>(Q, qb, ld, ncols, h2, k, 1, Wb, Wb, ld, n, p, true, true, partials,
-                               counters, norm, hsub, k * k, s));
+                               counters, norm, hsub, k * k, s, status));
     } else {
       MFG_LAUNCH(MFG_PROF_SUB, ub, pf + 2.0 * vecb / sizeof(T),
                  launch_sub<T>(Q, qb, ld, ncols, H + j, k * k, k, Wb, Wb, ld, n, p, true, true,
-                               partials, counters, norm, hsub, k * k, s));
+                               partials, counters, norm, hsub, k * k, s, status));
     }
     if (!last)
       MFG_LAUNCH(MFG_PROF_SCALE, 2.0 * vecb + bfb, vecb / sizeof(T),
@@ -414,7 +414,7 @@ static int run_adjoint(const mfg_operator *op, int64_t k, int64_t p, int64_t ld,
   // gamma = dH e_K - Q^T dr ;  lambda = dr + Q gamma   (decomp.py:498-499)
   if (dr) {
     MFG_LAUNCH(MFG_PROF_PROJ, (k + 1.0) * vecb, 2.0 * k * vecb / sizeof(T),
-               launch_proj<T>(Q, qb, ld, (int)k, dr, ld, n, p, partials, counters, h, k, 1, s));
+               launch_proj<T>(Q, qb, ld, (int)k, dr, ld, n, p, partials, counters, h, k, 1, s, status));
     MFG_CUDA_TRY(cudaMemcpy2DAsync(lam, ld * sizeof(T), dr, ld * sizeof(T), ld * sizeof(T), p,
                                    cudaMemcpyDeviceToDevice, s));
   }
@@ -422,24 +422,24 @@ static int run_adjoint(const mfg_operator *op, int64_t k, int64_t p, int64_t ld,
              launch_adj_init(dH, dr ? h : nullptr, (int)k, p, gamma, coef, s));
   MFG_LAUNCH(MFG_PROF_SUB, (k + 2.0) * vecb, 2.0 * k * vecb / sizeof(T),
              launch_sub<T>(Q, qb, ld, (int)k, coef, k, 1, lam, lam, ld, n, p, false, true, partials,
-                           counters, nullptr, nullptr, 0, s));
+                           counters, nullptr, nullptr, 0, s, status));
 
   for (int64_t idx = k - 1; idx >= 0; --idx) {
     const int ncr = (int)(idx + 2 < k ? idx + 2 : k);
     // masked re-projection: lambda -= Q_m (Q_m^T lambda - dH[:, idx]_m)   (decomp.py:576-584)
     MFG_LAUNCH(MFG_PROF_PROJ, (ncr + 1.0) * vecb, 2.0 * ncr * vecb / sizeof(T),
-               launch_proj<T>(Q, qb, ld, ncr, lam, ld, n, p, partials, counters, h, k, 1, s));
+               launch_proj<T>(Q, qb, ld, ncr, lam, ld, n, p, partials, counters, h, k, 1, s, status));
     MFG_LAUNCH(MFG_PROF_OTHER, 16.0 * p * ncr, (double)p * ncr,
                launch_adj_reortho_coef(h, dH, (int)k, p, (int)idx, ncr, coef, s));
     MFG_LAUNCH(MFG_PROF_SUB, (ncr + 2.0) * vecb, 2.0 * ncr * vecb / sizeof(T),
                launch_sub<T>(Q, qb, ld, ncr, coef, k, 1, lam, lam, ld, n, p, false, true, partials,
-                             counters, nullptr, nullptr, 0, s));
+                             counters, nullptr, nullptr, 0, s, status));
     // U = A^T lambda (= A lambda: tridiag_sym's operators are symmetric)   (decomp.py:587-589)
     if (hi) MFG_TRY(launch_split_bf16((const float *)lam, p, n, ld, hi, lo, ld, s));
     MFG_LAUNCH(MFG_PROF_APPLY, ab, af, apply_op<T>(op, lam, ld, U, ld, p, hi, lo, ld, panel, status, s));
     // Gamma row idx, (Gamma + Gamma^T)[idx, :], beta_plus row   (decomp.py:592-599)
     MFG_LAUNCH(MFG_PROF_PROJ, (idx + 2.0) * vecb, 2.0 * (idx + 1.0) * vecb / sizeof(T),
-               launch_proj<T>(Q, qb, ld, (int)(idx + 1), U, ld, n, p, partials, counters, g, k, 1, s));
+               launch_proj<T>(Q, qb, ld, (int)(idx + 1), U, ld, n, p, partials, counters, g, k, 1, s, status));
     MFG_LAUNCH(MFG_PROF_OTHER, 40.0 * p * k, 4.0 * p * k,
                launch_adj_step_coef(H, Pi, g, gamma, (int)k, p, (int)idx, Gamma, coef, bp, scal,
                                     beta, s));
@@ -450,12 +450,12 @@ static int run_adjoint(const mfg_operator *op, int64_t k, int64_t p, int64_t ld,
                launch_adj_lincomb<T>(U, lam, R, scal, n, ld, p, lam2, s));
     MFG_LAUNCH(MFG_PROF_SUB, (k + 2.0) * vecb, 2.0 * k * vecb / sizeof(T),
                launch_sub<T>(Q, qb, ld, (int)k, coef, k, 1, lam2, lam2, ld, n, p, false, true,
-                             partials, counters, nullptr, nullptr, 0, s));
+                             partials, counters, nullptr, nullptr, 0, s, status));
     if (idx + 1 < k) {
       const int nb = (int)(k - idx - 1);
       MFG_LAUNCH(MFG_PROF_SUB, (nb + 2.0) * vecb, 2.0 * nb * vecb / sizeof(T),
                  launch_sub<T>(Lam + (idx + 1) * ld, qb, ld, nb, bp + idx + 1, k, 1, lam2, lam2, ld,
-                               n, p, false, true, partials, counters, nullptr, nullptr, 0, s));
+                               n, p, false, true, partials, counters, nullptr, nullptr, 0, s, status));
     }
     MFG_LAUNCH(MFG_PROF_SCALE, 2.0 * vecb, vecb / sizeof(T),
                launch_scale<T>(lam2, ld, n, p, beta, lam, ld, nullptr, nullptr, 0, s));

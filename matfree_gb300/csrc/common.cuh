@@ -43,6 +43,64 @@ constexpr int kWarps = kThreads / 32;
 inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
 
 inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// ---------------------------------------------------------------------------
+// mbarrier waits, bounded in wall-clock time (%globaltimer) and given up
+// early when another role raised the CTA's failure flag.  Waits on the
+// critical path poll mbarrier.try_wait; waits of idle roles (an epilogue
+// waiting for the whole main loop) sleep in it with a suspend-time hint, so
+// they take no issue slots from the warps doing the work.
+// ---------------------------------------------------------------------------
+
+constexpr uint64_t kMbarWaitNs = 2000000000ull;  // 2 s: far beyond any copy or MMA
+constexpr uint32_t kMbarSleepNs = 1000000u;      // per sleeping try_wait
+
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+template <bool kSleep>
+__device__ __forceinline__ bool mbar_try_wait_parity(uint32_t bar_saddr, uint32_t parity) {
+  uint32_t ok;
+  if constexpr (kSleep) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(bar_saddr), "r"(parity), "r"(kMbarSleepNs)
+        : "memory");
+  } else {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(bar_saddr), "r"(parity)
+        : "memory");
+  }
+  return ok != 0;
+}
+
+// True once the phase of the barrier at shared address `bar_saddr` with the
+// given parity has completed; false after `limit_ns` or when *fail (if given)
+// becomes non-zero.
+template <bool kSleep = false>
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar_saddr, uint32_t parity,
+                                                  volatile int *fail,
+                                                  uint64_t limit_ns = kMbarWaitNs) {
+  if (mbar_try_wait_parity<kSleep>(bar_saddr, parity)) return true;
+  const uint64_t t0 = global_ns();
+  for (uint32_t it = 1;; ++it) {
+    if (mbar_try_wait_parity<kSleep>(bar_saddr, parity)) return true;
+    if (kSleep || (it & 63u) == 0) {
+      if (fail && *fail) return false;
+      if (global_ns() - t0 > limit_ns) return false;
+    }
+  }
+}
 inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 // 16-byte vector type per element type: 4 floats or 2 doubles.

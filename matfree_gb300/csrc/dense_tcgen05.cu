@@ -42,7 +42,6 @@ constexpr int kRowBytes = kBK * 2;  // 64-byte rows -> SWIZZLE_64B (128 -> SWIZZ
 static_assert(kRowBytes == 64 || kRowBytes == 128, "supported swizzle widths");
 constexpr int kUmmaK = 16;          // K per tcgen05.mma of kind::f16
 constexpr int kGemmThreads = 192;
-constexpr uint32_t kWaitLimit = 1u << 24;  // bounded spin on every mbarrier
 
 struct GemmShared {
   uint64_t full[8];
@@ -66,27 +65,16 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t by
                : "memory");
 }
 
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}\n"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-// Bounded wait; gives up early when another role raised the abort flag.
+// Bounded, sleeping wait; gives up early when another role raised the abort
+// flag, and raises it (with MFG_ERR_TIMEOUT) when the time limit runs out.
+template <bool kSleep = false>
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort_flag,
                                           int *status) {
-  for (uint32_t it = 0; it < kWaitLimit; ++it) {
-    if (mbar_try_wait(bar, parity)) return true;
-    if ((it & 1023u) == 1023u && *abort_flag) return false;
+  if (mbar_wait_bounded<kSleep>(smem_u32(bar), parity, abort_flag)) return true;
+  if (!*abort_flag) {
+    *abort_flag = 1;
+    if (status) atomicExch(status, (int)MFG_ERR_TIMEOUT);
   }
-  *abort_flag = 1;
-  if (status) atomicExch(status, (int)MFG_ERR_TIMEOUT);
   return false;
 }
 
@@ -223,8 +211,7 @@ dense_tcgen05_kernel(const __grid_constant__ CUtensorMap map_ahi,
         for (int kt = (issued > stages ? issued - stages : 0); kt < issued; ++kt) {
           const int s = kt % stages;
           const uint32_t ph = (uint32_t)(kt / stages) & 1u;
-          for (uint32_t it = 0; it < kWaitLimit && !mbar_try_wait(&sh->full[s], ph); ++it) {
-          }
+          mbar_wait_bounded(smem_u32(&sh->full[s]), ph, nullptr, kMbarWaitNs / 8);
         }
       }
     }
@@ -256,8 +243,7 @@ dense_tcgen05_kernel(const __grid_constant__ CUtensorMap map_ahi,
       // every MMA issued so far completes before this arrives
       umma_commit(done == num_k ? &sh->tmem_full : &sh->drain);
       if (done != num_k) {
-        for (uint32_t it = 0; it < kWaitLimit && !mbar_try_wait(&sh->drain, 0); ++it) {
-        }
+        mbar_wait_bounded(smem_u32(&sh->drain), 0, nullptr, kMbarWaitNs / 8);
       }
     }
   } else {
@@ -266,7 +252,8 @@ dense_tcgen05_kernel(const __grid_constant__ CUtensorMap map_ahi,
     const int row = quarter * 32 + lane;
     const int m = m0 + row;
     // warp-uniform decision: tcgen05.ld is executed by all 32 lanes or none
-    const bool ok = __all_sync(0xffffffffu, mbar_wait(&sh->tmem_full, 0, abort_flag, status));
+    // the epilogue sleeps through the main loop
+    const bool ok = __all_sync(0xffffffffu, mbar_wait<true>(&sh->tmem_full, 0, abort_flag, status));
     tc_fence_after();
     if (ok) {
       for (int c = 0; c < BN; c += 16) {

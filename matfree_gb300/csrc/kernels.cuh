@@ -13,13 +13,14 @@ template <typename T> int64_t num_chunks(int64_t n);
 template <typename T>
 int launch_proj(const T *Q, int64_t q_bstride, int64_t q_istride, int ncols, const T *Wv,
                 int64_t w_bstride, int64_t n, int64_t p, double *partials, unsigned *counters,
-                double *out, int64_t out_bstride, int64_t out_istride, cudaStream_t s);
+                double *out, int64_t out_bstride, int64_t out_istride, cudaStream_t s,
+                int *status = nullptr);
 template <typename T>
 int launch_sub(const T *Q, int64_t q_bstride, int64_t q_istride, int ncols, const double *coef,
                int64_t c_bstride, int64_t c_istride, const T *Win, T *Wout, int64_t w_bstride,
                int64_t n, int64_t p, bool with_norm, bool store, double *partials,
                unsigned *counters, double *norm_out, double *norm_out2, int64_t norm2_bstride,
-               cudaStream_t s);
+               cudaStream_t s, int *status = nullptr);
 template <typename T> int sub_proj_rows_per_thread(int ncols);
 template <typename T> int64_t max_fused_chunks(int64_t n);
 template <typename T>

@@ -267,7 +267,6 @@ __device__ __forceinline__ uint32_t smem_addr(const void *p) {
   return (uint32_t)__cvta_generic_to_shared(p);
 }
 
-constexpr uint32_t kBarWaitLimit = 1u << 24;
 constexpr int kSPGroup = 8;  // basis vectors per 2-D tensor copy
 
 // ---------------------------------------------------------------------------
@@ -424,20 +423,6 @@ int64_t num_chunks(int64_t n) { return ceil_div(n, chunk_rows<T>()); }
 template int64_t num_chunks<float>(int64_t);
 template int64_t num_chunks<double>(int64_t);
 
-template <typename T>
-int launch_proj(const T *Q, int64_t q_bstride, int64_t q_istride, int ncols, const T *Wv,
-                int64_t w_bstride, int64_t n, int64_t p, double *partials, unsigned *counters,
-                double *out, int64_t out_bstride, int64_t out_istride, cudaStream_t s) {
-  if (ncols <= 0 || p <= 0) return MFG_OK;
-  const int64_t nch = num_chunks<T>(n);
-  if (p > 65535 || ncols > kMaxProjCols) return MFG_ERR_UNSUPPORTED;
-  dim3 grid((unsigned)nch, (unsigned)p);
-  const size_t smem = (size_t)ncols * kWarps * sizeof(double);
-  proj_kernel<T><<<grid, kThreads, smem, s>>>(Q, q_bstride, q_istride, ncols, Wv, w_bstride, n,
-                                              (int)nch, partials, counters, out, out_bstride,
-                                              out_istride);
-  return MFG_LAUNCH_STATUS();
-}
 
 // ---------------------------------------------------------------------------
 // Fused second pass of CGS2: w' = w - Q h1 and h2 = Q^T w' from one read of
@@ -461,23 +446,11 @@ int launch_proj(const T *Q, int64_t q_bstride, int64_t q_istride, int ncols, con
 // multiple of 8 with zero columns that no copy writes.
 // ---------------------------------------------------------------------------
 
-// Bounded wait for the phase of `bar` with the given parity; every 1024
-// polls it gives up early if `fail` (when given) is set.
+// Bounded, sleeping wait for the phase of `bar` with the given parity.
 __device__ __forceinline__ bool bar_wait_bounded(uint64_t *bar, uint32_t parity,
                                                  volatile int *fail,
-                                                 uint32_t limit = kBarWaitLimit) {
-  for (uint32_t it = 0; it < limit; ++it) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}\n"
-        : "=r"(ok)
-        : "r"(smem_addr(bar)), "r"(parity)
-        : "memory");
-    if (ok) return true;
-    if (fail && (it & 1023u) == 1023u && *fail) return false;
-  }
-  return false;
+                                                 uint64_t limit_ns = kMbarWaitNs) {
+  return mbar_wait_bounded(smem_addr(bar), parity, fail, limit_ns);
 }
 
 constexpr int kSThreads = 128;
@@ -531,17 +504,27 @@ __device__ __forceinline__ int64_t cta_of_chunk(int64_t f, int64_t F, int64_t G)
   return ((f + 1) * G - 1) / F;
 }
 
-template <typename T, int MAXG, bool kHold>
+// What one pass of the streamed kernel computes per probe:
+//   kStreamSubProj  w' = w - Q c (stored), h_i = q_i . w'      (second CGS2 pass)
+//   kStreamProj     h_i = q_i . w                              (first CGS2 pass)
+//   kStreamSubNorm  w' = w - Q c (stored), ||w'||              (final CGS2 update)
+enum : int { kStreamSubProj = 0, kStreamProj = 1, kStreamSubNorm = 2 };
+
+template <typename T, int MAXG, bool kHold, int kMode>
 __global__ void __launch_bounds__(kSThreads + 32)
-sub_proj_stream_kernel(const __grid_constant__ CUtensorMap qmap, const T *__restrict__ Q,
-                       int64_t q_bstride, int64_t q_istride, int ncols,
-                       const double *__restrict__ coef, int64_t c_bstride, int64_t c_istride,
-                       T *Wv, int64_t w_bstride, int64_t n, int64_t p, int nbuf, int pstride,
-                       double *__restrict__ partials, unsigned *__restrict__ counters,
-                       double *__restrict__ out, int64_t out_bstride, int *__restrict__ status) {
+stream_sweep_kernel(const __grid_constant__ CUtensorMap qmap, const T *__restrict__ Q,
+                    int64_t q_bstride, int64_t q_istride, int ncols,
+                    const double *__restrict__ coef, int64_t c_bstride, int64_t c_istride,
+                    T *Wv, int64_t w_bstride, int64_t n, int64_t p, int nbuf, int pstride,
+                    double *__restrict__ partials, unsigned *__restrict__ counters,
+                    double *__restrict__ out, int64_t out_bstride, int64_t out_istride,
+                    double *__restrict__ out2, int64_t out2_bstride, int *__restrict__ status) {
+  constexpr bool kUpdate = kMode != kStreamProj;   // forms w' = w - Q c
+  constexpr bool kDots = kMode != kStreamSubNorm;  // sums q_i . (w or w')
   extern __shared__ __align__(128) uint8_t smem[];
   const int ngroups = (ncols + kSPGroup - 1) / kSPGroup;
   const int cpad = ngroups * kSPGroup;
+  const int nout = kDots ? ncols : 1;
   // ring of nbuf buffers [cpad + 1][kSR]: the chunk's basis rows (zero
   // columns past ncols), then its rows of w
   T *bufs = reinterpret_cast<T *>(smem);
@@ -588,18 +571,21 @@ sub_proj_stream_kernel(const __grid_constant__ CUtensorMap qmap, const T *__rest
     // copies c, c + 32, ...
     int issued = 0;
     const int ncopies = full + (ncols - full * kSPGroup) + 1;
-    for (int64_t f = f_begin; f < f_end; ++f) {
-      const int t = (int)(f - f_begin);
-      const int u = t % nbuf;
-      if (t >= nbuf && !bar_wait_bounded(&empty_bar[u], (uint32_t)((t / nbuf - 1) & 1), fail)) {
+    // position of chunk t: probe b, row chunk c, buffer u used for the
+    // (ph)-parity time; advanced without divisions
+    int64_t b = f_begin / C, c = f_begin - (f_begin / C) * C;
+    int u = 0;
+    uint32_t ph = 0;
+    const int nt = (int)(f_end - f_begin);
+    for (int t = 0; t < nt; ++t) {
+      if (t >= nbuf && !bar_wait_bounded(&empty_bar[u], ph ^ 1u, fail)) {
         if (lane == 0) {
           *fail = 1;
           if (status) atomicExch(status, (int)MFG_ERR_TIMEOUT);
         }
         break;
       }
-      const int64_t b = f / C;
-      const int64_t r0 = (f - b * C) * kSR;
+      const int64_t r0 = c * kSR;
       const int64_t rows = (n - r0 < kSR) ? (n - r0) : kSR;
       const uint32_t seg_bytes = (uint32_t)(((rows * (int64_t)sizeof(T)) + 15) / 16 * 16);
       const uint32_t bytes = (uint32_t)full * (uint32_t)(kSPGroup * kSR * sizeof(T)) +
@@ -633,112 +619,138 @@ sub_proj_stream_kernel(const __grid_constant__ CUtensorMap qmap, const T *__rest
         }
       }
       issued = t + 1;
+      if (++c == C) {
+        c = 0;
+        ++b;
+      }
+      if (++u == nbuf) {
+        u = 0;
+        ph ^= 1u;
+      }
     }
     if (*fail && lane == 0) {
       // the copies of the last chunks issued land (bounded) before the CTA's
       // shared memory goes away; earlier buffers were consumed before reuse
       for (int t = (issued > nbuf ? issued - nbuf : 0); t < issued; ++t)
-        bar_wait_bounded(&full_bar[t % nbuf], (uint32_t)((t / nbuf) & 1), nullptr, kBarWaitLimit >> 4);
+        bar_wait_bounded(&full_bar[t % nbuf], (uint32_t)((t / nbuf) & 1), nullptr, kMbarWaitNs / 8);
     }
   } else {
     // row warps: thread j owns row j of every chunk
     const int j = threadIdx.x;
-    T acc[kSPGroup * MAXG];
+    T acc[kDots ? kSPGroup * MAXG : 1];
 #pragma unroll
-    for (int i = 0; i < kSPGroup * MAXG; ++i) acc[i] = (T)0;
-    int64_t b = -1;
-    for (int64_t f = f_begin; f < f_end; ++f) {
-      const int t = (int)(f - f_begin);
-      const int u = t % nbuf;
-      if (b != f / C) {
-        // a new probe: its coefficients (the row warps are past every read
-        // of the previous ones)
-        row_warps_sync();
-        b = f / C;
-        for (int i = j; i < cpad; i += kSThreads)
-          s_coef[i] = i < ncols ? (T)coef[b * c_bstride + i * c_istride] : (T)0;
-        row_warps_sync();
+    for (int i = 0; i < (kDots ? kSPGroup * MAXG : 1); ++i) acc[i] = (T)0;
+    double nrm = 0.0;  // ||w'||^2 over this thread's rows (kStreamSubNorm)
+    int64_t b = f_begin / C, c = f_begin - (f_begin / C) * C;
+    int u = 0;
+    uint32_t ph = 0;
+    const int nt = (int)(f_end - f_begin);
+    for (int t = 0; t < nt; ++t) {
+      if (t == 0 || c == 0) {
+        if constexpr (kUpdate) {
+          // a new probe: its coefficients (the row warps are past every read
+          // of the previous ones)
+          row_warps_sync();
+          for (int i = j; i < cpad; i += kSThreads)
+            s_coef[i] = i < ncols ? (T)coef[b * c_bstride + i * c_istride] : (T)0;
+          row_warps_sync();
+        }
       }
       // After a failure every row warp still walks the remaining chunks
       // (without waiting or computing), so all of them meet at the same
       // named barriers.
       bool ready = false;
       if (!*fail) {
-        ready = bar_wait_bounded(&full_bar[u], (uint32_t)((t / nbuf) & 1), fail);
+        ready = bar_wait_bounded(&full_bar[u], ph, fail);
         if (!ready) {
           *fail = 1;
           if (status) atomicExch(status, (int)MFG_ERR_TIMEOUT);
         }
       }
       const T *buf = bufs + u * bstr + j;  // this thread's row, column stride kSR
-      const int64_t r0 = (f - b * C) * kSR;
+      const int64_t r0 = c * kSR;
       const int rows = (int)((n - r0 < kSR) ? (n - r0) : kSR);
-      // w' = w - Q c over this thread's row; four interleaved sums shorten
-      // the dependent chain
       T qv[kHold ? kSPGroup * MAXG : 1];
-      T w0 = ready ? buf[(size_t)cpad * kSR] : (T)0, w1 = (T)0, w2 = (T)0, w3 = (T)0;
-#pragma unroll
-      for (int g = 0; g < MAXG; ++g)
-        if (ready && g < ngroups) {
-#pragma unroll
-          for (int e = 0; e < kSPGroup; e += 4) {
-            const int i = g * kSPGroup + e;
-            const T q0 = buf[(size_t)i * kSR], q1 = buf[(size_t)(i + 1) * kSR];
-            const T q2 = buf[(size_t)(i + 2) * kSR], q3 = buf[(size_t)(i + 3) * kSR];
-            if constexpr (kHold) {
-              qv[i] = q0;
-              qv[i + 1] = q1;
-              qv[i + 2] = q2;
-              qv[i + 3] = q3;
-            }
-            w0 = fma(-q0, s_coef[i], w0);
-            w1 = fma(-q1, s_coef[i + 1], w1);
-            w2 = fma(-q2, s_coef[i + 2], w2);
-            w3 = fma(-q3, s_coef[i + 3], w3);
-          }
-        }
-      const T w = (w0 + w1) + (w2 + w3);
-      // rows past the probe's end hold stale shared memory and are left out
-      if (ready && j < rows) {
-        Wv[b * w_bstride + r0 + j] = w;
+      T w = ready ? buf[(size_t)cpad * kSR] : (T)0;
+      if constexpr (kUpdate) {
+        // w' = w - Q c over this thread's row; four interleaved sums shorten
+        // the dependent chain
+        T w0 = w, w1 = (T)0, w2 = (T)0, w3 = (T)0;
 #pragma unroll
         for (int g = 0; g < MAXG; ++g)
-          if (g < ngroups) {
+          if (ready && g < ngroups) {
 #pragma unroll
-            for (int e = 0; e < kSPGroup; ++e) {
+            for (int e = 0; e < kSPGroup; e += 4) {
               const int i = g * kSPGroup + e;
-              const T q = kHold ? qv[kHold ? i : 0] : buf[(size_t)i * kSR];
-              acc[i] = fma(q, w, acc[i]);
+              const T q0 = buf[(size_t)i * kSR], q1 = buf[(size_t)(i + 1) * kSR];
+              const T q2 = buf[(size_t)(i + 2) * kSR], q3 = buf[(size_t)(i + 3) * kSR];
+              if constexpr (kHold) {
+                qv[i] = q0;
+                qv[i + 1] = q1;
+                qv[i + 2] = q2;
+                qv[i + 3] = q3;
+              }
+              w0 = fma(-q0, s_coef[i], w0);
+              w1 = fma(-q1, s_coef[i + 1], w1);
+              w2 = fma(-q2, s_coef[i + 2], w2);
+              w3 = fma(-q3, s_coef[i + 3], w3);
             }
           }
+        w = (w0 + w1) + (w2 + w3);
+      }
+      // rows past the probe's end hold stale shared memory and are left out
+      if (ready && j < rows) {
+        if constexpr (kUpdate) Wv[b * w_bstride + r0 + j] = w;
+        if constexpr (kMode == kStreamSubNorm) {
+          const T w2 = w * w;
+          nrm += (double)w2;
+        }
+        if constexpr (kDots) {
+#pragma unroll
+          for (int g = 0; g < MAXG; ++g)
+            if (g < ngroups) {
+#pragma unroll
+              for (int e = 0; e < kSPGroup; ++e) {
+                const int i = g * kSPGroup + e;
+                const T q = kHold ? qv[kHold ? i : 0] : buf[(size_t)i * kSR];
+                acc[i] = fma(q, w, acc[i]);
+              }
+            }
+        }
       }
       __syncwarp();
       if (lane == 0 && ready)
         asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(&empty_bar[u])) : "memory");
 
-      // the probe's last row chunk in this CTA: its share of h2
-      if (f + 1 == f_end || (f + 1) / C != b) {
-        warp_xsum<T, kSPGroup * MAXG>(acc, lane);
-        constexpr int kPer = (kSPGroup * MAXG) / 32 > 0 ? (kSPGroup * MAXG) / 32 : 1;
-        constexpr int kDup = (kSPGroup * MAXG) >= 32 ? 1 : 32 / (kSPGroup * MAXG);
-        if ((lane & (kDup - 1)) == 0) {
+      // the probe's last row chunk in this CTA: its share of the outputs
+      if (t + 1 == nt || c + 1 == C) {
+        if constexpr (kDots) {
+          // per-thread float sums -> warp butterfly -> fixed-order warp sum
+          warp_xsum<T, kSPGroup * MAXG>(acc, lane);
+          constexpr int kPer = (kSPGroup * MAXG) / 32 > 0 ? (kSPGroup * MAXG) / 32 : 1;
+          constexpr int kDup = (kSPGroup * MAXG) >= 32 ? 1 : 32 / (kSPGroup * MAXG);
+          if ((lane & (kDup - 1)) == 0) {
 #pragma unroll
-          for (int i = 0; i < kPer; ++i) red[warp][xsum_index<kSPGroup * MAXG>(lane, i)] = (double)acc[i];
+            for (int i = 0; i < kPer; ++i) red[warp][xsum_index<kSPGroup * MAXG>(lane, i)] = (double)acc[i];
+          }
+#pragma unroll
+          for (int i = 0; i < kSPGroup * MAXG; ++i) acc[i] = (T)0;
+        } else {
+          const double v = warp_sum(nrm);
+          if (lane == 0) red[warp][0] = v;
+          nrm = 0.0;
         }
-#pragma unroll
-        for (int i = 0; i < kSPGroup * MAXG; ++i) acc[i] = (T)0;
         row_warps_sync();
         double h = 0.0;
-        if (j < ncols) {
+        if (j < nout) {
 #pragma unroll
           for (int q = 0; q < kSWarps; ++q) h += red[q][j];
         }
         const int64_t first = cta_of_chunk(b * C, F, G), last = cta_of_chunk(b * C + C - 1, F, G);
-        if (first == last) {
-          if (j < ncols) out[b * out_bstride + j] = h;
-        } else {
+        bool emit = first == last;
+        if (!emit) {
           const int64_t seg = (int64_t)blockIdx.x - first;
-          if (j < ncols) partials[(b * pstride + seg) * ncols + j] = h;
+          if (j < nout) partials[(b * pstride + seg) * nout + j] = h;
           __threadfence();
           row_warps_sync();
           if (j == 0) {
@@ -748,17 +760,34 @@ sub_proj_stream_kernel(const __grid_constant__ CUtensorMap qmap, const T *__rest
           row_warps_sync();
           if (s_last) {
             __threadfence();
-            if (j < ncols) {
-              double v = 0.0;
+            emit = true;
+            if (j < nout) {
+              h = 0.0;
               for (int64_t q = 0; q <= last - first; ++q)
-                v += __ldcg(&partials[(b * pstride + q) * ncols + j]);
-              out[b * out_bstride + j] = v;
+                h += __ldcg(&partials[(b * pstride + q) * nout + j]);
             }
             if (j == 0) counters[b] = 0u;
           }
         }
+        if (emit && j < nout) {
+          if constexpr (kMode == kStreamSubNorm) {
+            const double nv = sqrt(h);
+            out[b * out_bstride] = nv;
+            if (out2) out2[b * out2_bstride] = nv;
+          } else {
+            out[b * out_bstride + j * out_istride] = h;
+          }
+        }
         // red and s_last are reused at this CTA's next probe
         row_warps_sync();
+      }
+      if (++c == C) {
+        c = 0;
+        ++b;
+      }
+      if (++u == nbuf) {
+        u = 0;
+        ph ^= 1u;
       }
     }
   }
@@ -766,36 +795,49 @@ sub_proj_stream_kernel(const __grid_constant__ CUtensorMap qmap, const T *__rest
 }
 
 template <typename T>
-static size_t sub_proj_stream_smem(int ncols, int nbuf) {
+static size_t stream_sweep_smem(int ncols, int nbuf) {
   const int cpad = (ncols + kSPGroup - 1) / kSPGroup * kSPGroup;
   return (size_t)nbuf * (cpad + 1) * kSR * sizeof(T) + (size_t)cpad * sizeof(T);
 }
 
-// Largest vector count of the streamed kernel: 128 floats, 64 doubles (the
-// per-thread sums live in registers).
-template <typename T> constexpr int sub_proj_stream_max_cols() { return sizeof(T) == 4 ? 128 : 64; }
+// Largest vector count of the streamed sweeps: 128 floats, 64 doubles (the
+// per-thread dot-product sums live in registers).
+template <typename T> constexpr int stream_sweep_max_cols() { return sizeof(T) == 4 ? 128 : 64; }
 
 // Ring depth: as many buffers (2..8) as fit in ~110 KB, so that two CTAs
-// share an SM; 0 if even two do not fit in ~220 KB.
+// share an SM; 0 if the sweep does not apply.
 template <typename T>
-static int sub_proj_stream_buffers(int ncols) {
-  if (ncols < 1 || ncols > sub_proj_stream_max_cols<T>()) return 0;
+static int stream_sweep_buffers(int ncols) {
+  if (ncols < 1 || ncols > stream_sweep_max_cols<T>()) return 0;
   int nb = kSMaxBuf;
-  while (nb > 2 && sub_proj_stream_smem<T>(ncols, nb) > 110 * 1024) --nb;
-  return sub_proj_stream_smem<T>(ncols, nb) <= 220 * 1024 ? nb : 0;
+  while (nb > 2 && stream_sweep_smem<T>(ncols, nb) > 110 * 1024) --nb;
+  return stream_sweep_smem<T>(ncols, nb) <= 220 * 1024 ? nb : 0;
 }
 
-template <typename T, int MAXG, bool kHold>
-static int launch_sub_proj_stream_t(const T *Q, int64_t q_bstride, int64_t q_istride, int ncols,
-                                    const double *coef, int64_t c_bstride, int64_t c_istride,
-                                    T *Wv, int64_t w_bstride, int64_t n, int64_t p,
-                                    double *partials, unsigned *counters, double *out,
-                                    int64_t out_bstride, int *status, cudaStream_t s) {
-  const int nbuf = sub_proj_stream_buffers<T>(ncols);
+struct StreamArgs {
+  const void *Q;
+  int64_t q_bstride, q_istride;
+  int ncols;
+  const double *coef;
+  int64_t c_bstride, c_istride;
+  void *Wv;
+  int64_t w_bstride, n, p;
+  double *partials;
+  unsigned *counters;
+  double *out;
+  int64_t out_bstride, out_istride;
+  double *out2;
+  int64_t out2_bstride;
+  int *status;
+};
+
+template <typename T, int MAXG, bool kHold, int kMode>
+static int launch_stream_sweep_t(const StreamArgs &a, cudaStream_t s) {
+  const int nbuf = stream_sweep_buffers<T>(a.ncols);
   if (nbuf < 2) return MFG_ERR_UNSUPPORTED;
-  const size_t smem = sub_proj_stream_smem<T>(ncols, nbuf);
-  if (q_istride <= 0 || q_bstride % q_istride != 0) return MFG_ERR_BAD_ARG;
-  auto kern = sub_proj_stream_kernel<T, MAXG, kHold>;
+  const size_t smem = stream_sweep_smem<T>(a.ncols, nbuf);
+  if (a.q_istride <= 0 || a.q_bstride % a.q_istride != 0) return MFG_ERR_BAD_ARG;
+  auto kern = stream_sweep_kernel<T, MAXG, kHold, kMode>;
   // The default dynamic limit is 48 KB minus the kernel's static shared
   // memory, so the opt-in is raised well below 48 KB.
   if (smem > 32 * 1024)
@@ -809,60 +851,57 @@ static int launch_sub_proj_stream_t(const T *Q, int64_t q_bstride, int64_t q_ist
     MFG_CUDA_TRY(cudaGetDevice(&dev));
     MFG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   }
-  int per_sm = per_sm_cache[ncols];
+  int per_sm = per_sm_cache[a.ncols];
   if (per_sm == 0) {
     MFG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kSThreads + 32, smem));
     if (per_sm < 1) return MFG_ERR_UNSUPPORTED;
-    per_sm_cache[ncols] = per_sm;
+    per_sm_cache[a.ncols] = per_sm;
   }
   // One wave of CTAs, each with an equal share of the p * C row chunks.  A
   // probe then spans at most ceil(G / p) + 1 CTAs, whose partial sums must
   // fit the workspace's max_fused_chunks(n) slots per probe.
-  const int64_t C = ceil_div(n, kSR);
-  const int64_t F = p * C;
-  const int64_t cap = max_fused_chunks<T>(n);
+  const int64_t C = ceil_div(a.n, kSR);
+  const int64_t F = a.p * C;
+  const int64_t cap = max_fused_chunks<T>(a.n);
   int64_t G = (int64_t)sms * per_sm;
   if (G > F) G = F;
-  if (G > p * (cap - 1)) G = p * (cap - 1);
+  if (G > a.p * (cap - 1)) G = a.p * (cap - 1);
   if (G < 1) G = 1;
-  const int pstride = (int)(ceil_div(G, p) + 1);
-  // the basis as rows of q_istride elements: row b * k + i is probe b's vector i
+  const int pstride = (int)(ceil_div(G, a.p) + 1);
+  // the basis as rows of q_istride elements: row b * k + i is probe b's
+  // vector i (only read through 2-D copies when there are 8 or more vectors)
   CUtensorMap qmap;
-  const int64_t kcols = q_bstride / q_istride;
-  if (!make_plain_tensor_map_2d(&qmap, (int)sizeof(T), Q, n, p * kcols, q_istride, (uint32_t)kSR,
-                                (uint32_t)kSPGroup))
+  memset(&qmap, 0, sizeof(qmap));
+  const int64_t kcols = a.q_bstride / a.q_istride;
+  if (a.ncols >= kSPGroup &&
+      !make_plain_tensor_map_2d(&qmap, (int)sizeof(T), a.Q, a.n, a.p * kcols, a.q_istride,
+                                (uint32_t)kSR, (uint32_t)kSPGroup))
     return MFG_ERR_CUDA;
-  kern<<<(unsigned)G, kSThreads + 32, smem, s>>>(qmap, Q, q_bstride, q_istride, ncols, coef,
-                                                 c_bstride, c_istride, Wv, w_bstride, n, p, nbuf,
-                                                 pstride, partials, counters, out, out_bstride,
-                                                 status);
+  kern<<<(unsigned)G, kSThreads + 32, smem, s>>>(
+      qmap, static_cast<const T *>(a.Q), a.q_bstride, a.q_istride, a.ncols, a.coef, a.c_bstride,
+      a.c_istride, static_cast<T *>(a.Wv), a.w_bstride, a.n, a.p, nbuf, pstride, a.partials,
+      a.counters, a.out, a.out_bstride, a.out_istride, a.out2, a.out2_bstride, a.status);
   return MFG_LAUNCH_STATUS();
 }
 
-template <typename T>
-static int launch_sub_proj_stream(const T *Q, int64_t q_bstride, int64_t q_istride, int ncols,
-                                  const double *coef, int64_t c_bstride, int64_t c_istride, T *Wv,
-                                  int64_t w_bstride, int64_t n, int64_t p, double *partials,
-                                  unsigned *counters, double *out, int64_t out_bstride, int *status,
-                                  cudaStream_t s) {
-  // register sums sized to the vector count (8, 32, 64 or 128 of them); up
-  // to 64 the basis values also stay in registers between the two passes
-#define MFG_SPS(G, H)                                                                            \
-  return launch_sub_proj_stream_t<T, G, H>(Q, q_bstride, q_istride, ncols, coef, c_bstride,     \
-                                           c_istride, Wv, w_bstride, n, p, partials, counters,  \
-                                           out, out_bstride, status, s)
-  if (ncols <= 8) MFG_SPS(1, true);
-  if (ncols <= 32) MFG_SPS(4, true);
-  if (ncols <= 64) MFG_SPS(8, sizeof(T) == 4);
-  if constexpr (sizeof(T) == 4) MFG_SPS(16, false);
-#undef MFG_SPS
+template <typename T, int kMode>
+static int launch_stream_sweep(const StreamArgs &a, cudaStream_t s) {
+  if (stream_sweep_buffers<T>(a.ncols) == 0) return MFG_ERR_UNSUPPORTED;
+  // loops (and, for dot products, register sums) sized to the vector count:
+  // 8, 32, 64 or 128; in the two-pass form up to 64 (32 doubles) basis
+  // values also stay in registers between the passes
+  constexpr bool kTwo = kMode == kStreamSubProj;
+  if (a.ncols <= 8) return launch_stream_sweep_t<T, 1, kTwo, kMode>(a, s);
+  if (a.ncols <= 32) return launch_stream_sweep_t<T, 4, kTwo, kMode>(a, s);
+  if (a.ncols <= 64) return launch_stream_sweep_t<T, 8, kTwo && sizeof(T) == 4, kMode>(a, s);
+  if constexpr (sizeof(T) == 4) return launch_stream_sweep_t<T, 16, false, kMode>(a, s);
   return MFG_ERR_UNSUPPORTED;
 }
 
 // 1 when the fused update+projection applies to this vector count, else 0.
 template <typename T>
 int sub_proj_rows_per_thread(int ncols) {
-  return sub_proj_stream_buffers<T>(ncols) > 0 ? 1 : 0;
+  return stream_sweep_buffers<T>(ncols) > 0 ? 1 : 0;
 }
 
 // Partial-sum slots per probe of the cross-CTA reductions (at least 2: the
@@ -878,9 +917,32 @@ int launch_sub_proj(const T *Q, int64_t q_bstride, int64_t q_istride, int ncols,
                     int64_t p, double *partials, unsigned *counters, double *out,
                     int64_t out_bstride, int *status, cudaStream_t s) {
   if (ncols <= 0 || p <= 0) return MFG_OK;
-  if (sub_proj_stream_buffers<T>(ncols) == 0) return MFG_ERR_UNSUPPORTED;
-  return launch_sub_proj_stream<T>(Q, q_bstride, q_istride, ncols, coef, c_bstride, c_istride, Wv,
-                                   w_bstride, n, p, partials, counters, out, out_bstride, status, s);
+  const StreamArgs a{Q,        q_bstride, q_istride, ncols, coef, c_bstride,   c_istride,
+                     Wv,       w_bstride, n,         p,     partials, counters, out,
+                     out_bstride, 1,      nullptr,   0,     status};
+  return launch_stream_sweep<T, kStreamSubProj>(a, s);
+}
+
+template <typename T>
+int launch_proj(const T *Q, int64_t q_bstride, int64_t q_istride, int ncols, const T *Wv,
+                int64_t w_bstride, int64_t n, int64_t p, double *partials, unsigned *counters,
+                double *out, int64_t out_bstride, int64_t out_istride, cudaStream_t s,
+                int *status) {
+  if (ncols <= 0 || p <= 0) return MFG_OK;
+  if (stream_sweep_buffers<T>(ncols) > 0) {
+    const StreamArgs a{Q,        q_bstride, q_istride,   ncols,       nullptr, 0,   0,
+                       const_cast<T *>(Wv), w_bstride,   n,           p,       partials,
+                       counters, out,       out_bstride, out_istride, nullptr, 0,   status};
+    return launch_stream_sweep<T, kStreamProj>(a, s);
+  }
+  const int64_t nch = num_chunks<T>(n);
+  if (p > 65535 || ncols > kMaxProjCols) return MFG_ERR_UNSUPPORTED;
+  dim3 grid((unsigned)nch, (unsigned)p);
+  const size_t smem = (size_t)ncols * kWarps * sizeof(double);
+  proj_kernel<T><<<grid, kThreads, smem, s>>>(Q, q_bstride, q_istride, ncols, Wv, w_bstride, n,
+                                              (int)nch, partials, counters, out, out_bstride,
+                                              out_istride);
+  return MFG_LAUNCH_STATUS();
 }
 
 template <typename T>
@@ -888,8 +950,14 @@ int launch_sub(const T *Q, int64_t q_bstride, int64_t q_istride, int ncols, cons
                int64_t c_bstride, int64_t c_istride, const T *Win, T *Wout, int64_t w_bstride,
                int64_t n, int64_t p, bool with_norm, bool store, double *partials,
                unsigned *counters, double *norm_out, double *norm_out2, int64_t norm2_bstride,
-               cudaStream_t s) {
+               cudaStream_t s, int *status) {
   if (p <= 0) return MFG_OK;
+  if (with_norm && store && Win == Wout && ncols > 0 && stream_sweep_buffers<T>(ncols) > 0) {
+    const StreamArgs a{Q,        q_bstride, q_istride, ncols,   coef,      c_bstride,    c_istride,
+                       Wout,     w_bstride, n,         p,       partials,  counters,     norm_out,
+                       1,        0,         norm_out2, norm2_bstride, status};
+    return launch_stream_sweep<T, kStreamSubNorm>(a, s);
+  }
   const int64_t nch = num_chunks<T>(n);
   if (p > 65535) return MFG_ERR_UNSUPPORTED;
   dim3 grid((unsigned)nch, (unsigned)p);
@@ -936,10 +1004,11 @@ int launch_inv(const double *x, double *y, int64_t p, cudaStream_t s) {
                                   unsigned *, double *, int64_t, int *, cudaStream_t);         \
   template int launch_proj<T>(const T *, int64_t, int64_t, int, const T *, int64_t, int64_t,   \
                               int64_t, double *, unsigned *, double *, int64_t, int64_t,       \
-                              cudaStream_t);                                                   \
+                              cudaStream_t, int *);                                            \
   template int launch_sub<T>(const T *, int64_t, int64_t, int, const double *, int64_t,        \
                              int64_t, const T *, T *, int64_t, int64_t, int64_t, bool, bool,   \
-                             double *, unsigned *, double *, double *, int64_t, cudaStream_t); \
+                             double *, unsigned *, double *, double *, int64_t, cudaStream_t,  \
+                             int *);                                                           \
   template int launch_scale<T>(const T *, int64_t, int64_t, int64_t, const double *, T *,      \
                                int64_t, __nv_bfloat16 *, __nv_bfloat16 *, int64_t, cudaStream_t);
 MFG_INST(float)
