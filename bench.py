@@ -40,6 +40,9 @@ CONFIGS = {
     "rbf8k": ("rbf", 8192, 16, 256),
     # same, with the bench depth k = 64 (basis 537 MB) for captures of late steps
     "rbf8k64": ("rbf", 8192, 64, 256),
+    # the bench's operator (n = 16384, 1.07 GB in bf16 hi + lo) at depth 4,
+    # for captures of the full-size operator apply
+    "rbf16k4": ("rbf", 16384, 4, 256),
     "dense1k": ("dense", 1000, 30, 100),
     "laplace1m": ("csr", 1024 * 1024, 100, 64),
 }

@@ -42,6 +42,7 @@ constexpr int kRowBytes = kBK * 2;  // 64-byte rows -> SWIZZLE_64B (128 -> SWIZZ
 static_assert(kRowBytes == 64 || kRowBytes == 128, "supported swizzle widths");
 constexpr int kUmmaK = 16;          // K per tcgen05.mma of kind::f16
 constexpr int kGemmThreads = 192;
+constexpr int64_t kPairMinRows = 1024;  // CTA pairs from this operator size on
 
 struct GemmShared {
   uint64_t full[8];
@@ -283,6 +284,221 @@ dense_tcgen05_kernel(const __grid_constant__ CUtensorMap map_ahi,
 }
 
 // ---------------------------------------------------------------------------
+// 2-SM form (tcgen05 cta_group::2): a cluster of two CTAs computes one tile
+// of 256 operator rows x BN probes.  Each CTA loads its own 128 rows of A
+// (hi, lo) and its own half of the panel tile (BN / 2 probes, hi, lo); the
+// pair's tensor cores exchange the panel halves, so every SM streams a third
+// fewer bytes per flop than the one-CTA form, and the smaller stages leave
+// room for a deeper ring.  All copies of a stage complete on the lead CTA's
+// "full" barrier (the lead arms it with both CTAs' bytes); the lead CTA's
+// MMA thread issues the M = 256 MMAs and its commits arrive on the "empty"
+// and "tmem_full" barriers of both CTAs.  Each CTA's epilogue reads its own
+// 128 TMEM lanes.
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+
+// shared::cluster address of the same shared variable in CTA `rank`
+__device__ __forceinline__ uint32_t map_to_rank(uint32_t saddr, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(saddr), "r"(rank));
+  return r;
+}
+
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+  asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+// 2-D tile copy into this CTA's shared memory completing on a barrier that
+// may live in the peer CTA (shared::cluster address).
+__device__ __forceinline__ void tma_load_2d_pair(void *dst, const CUtensorMap *map, uint32_t bar_cluster,
+                                                 int x, int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.cta_group::2.shared::cluster.global.mbarrier::complete_tx::bytes "
+      "[%0], [%1, {%3, %4}], [%2];"
+      ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(bar_cluster), "r"(x), "r"(y)
+      : "memory");
+}
+
+__device__ __forceinline__ void umma_bf16_pair(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
+                                               uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n\t}\n"
+      ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+// arrive on the barrier at the same offset in both CTAs of the pair once the
+// MMAs issued so far have completed
+__device__ __forceinline__ void umma_commit_pair(uint64_t *bar) {
+  const uint16_t mask = 0x3;
+  asm volatile(
+      "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;"
+      ::"r"(smem_u32(bar)), "h"(mask)
+      : "memory");
+}
+
+// arrive on this CTA's barrier only
+__device__ __forceinline__ void umma_commit_pair_local(uint64_t *bar) {
+  asm volatile("tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                   smem_u32(bar))
+               : "memory");
+}
+
+template <bool kSplit>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kGemmThreads, 1)
+dense_tcgen05_pair_kernel(const __grid_constant__ CUtensorMap map_ahi,
+                          const __grid_constant__ CUtensorMap map_alo,
+                          const __grid_constant__ CUtensorMap map_bhi,
+                          const __grid_constant__ CUtensorMap map_blo, const float *__restrict__ Vf,
+                          int64_t ldvf, float *__restrict__ W, int64_t ldw, int n, int p, int BN,
+                          int stages, uint32_t tmem_cols, float shift, int *status) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t *tiles = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+  const uint32_t a_bytes = kBM * kBK * 2;                 // this CTA's 128 operator rows
+  const uint32_t b_bytes = (uint32_t)(BN / 2) * kBK * 2;  // this CTA's half of the probe tile
+  const uint32_t stage_bytes = (kSplit ? 2u : 1u) * (a_bytes + b_bytes);
+  GemmShared *sh = reinterpret_cast<GemmShared *>(tiles + (size_t)stages * stage_bytes);
+
+  const uint32_t rank = cluster_rank();
+  const bool lead = rank == 0;
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const int m0 = (int)(blockIdx.x >> 1) * (2 * kBM) + (int)rank * kBM;
+  const int b0 = blockIdx.y * BN;
+  const int bh = b0 + (int)rank * (BN / 2);
+  const int num_k = (n + kBK - 1) / kBK;
+  volatile int *abort_flag = &sh->abort;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < stages; ++s) {
+      mbar_init(&sh->full[s], 1);
+      mbar_init(&sh->empty[s], 1);
+    }
+    mbar_init(&sh->tmem_full, 1);
+    mbar_init(&sh->drain, 1);
+    sh->abort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    // one warp of each CTA of the pair allocates, collectively
+    asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&sh->tmem_base)),
+                 "r"(tmem_cols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  // barriers of both CTAs are initialised before any copy or commit reaches them
+  cluster_sync_all();
+  tc_fence_after();
+  const uint32_t tmem = sh->tmem_base;
+  const uint32_t full0_lead = map_to_rank(smem_u32(&sh->full[0]), 0);
+
+  if (warp == 0) {
+    if (lane == 0) {
+      int issued = 0;
+      for (int kt = 0; kt < num_k; ++kt) {
+        const int s = kt % stages;
+        const uint32_t ph = (uint32_t)(kt / stages) & 1u;
+        if (!mbar_wait(&sh->empty[s], ph ^ 1u, abort_flag, status)) break;
+        uint8_t *st = tiles + (size_t)s * stage_bytes;
+        const uint32_t full_s = full0_lead + (uint32_t)(s * sizeof(uint64_t));
+        if (lead) mbar_arrive_expect_tx(&sh->full[s], 2u * stage_bytes);
+        const int kx = kt * kBK;
+        tma_load_2d_pair(st, &map_ahi, full_s, kx, m0);
+        tma_load_2d_pair(st + a_bytes, &map_bhi, full_s, kx, bh);
+        if (kSplit) {
+          tma_load_2d_pair(st + a_bytes + b_bytes, &map_alo, full_s, kx, m0);
+          tma_load_2d_pair(st + 2 * a_bytes + b_bytes, &map_blo, full_s, kx, bh);
+        }
+        ++issued;
+      }
+      // drain (lead CTA): the copies of both CTAs complete on its "full" barriers
+      if (*abort_flag && lead) {
+        for (int kt = (issued > stages ? issued - stages : 0); kt < issued; ++kt) {
+          const int s = kt % stages;
+          const uint32_t ph = (uint32_t)(kt / stages) & 1u;
+          mbar_wait_bounded(smem_u32(&sh->full[s]), ph, nullptr, kMbarWaitNs / 8);
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0 && lead) {
+      const uint32_t idesc = instr_desc_bf16(2 * kBM, BN);
+      int done = 0;
+      for (int kt = 0; kt < num_k; ++kt) {
+        const int s = kt % stages;
+        const uint32_t ph = (uint32_t)(kt / stages) & 1u;
+        if (!mbar_wait(&sh->full[s], ph, abort_flag, status)) break;
+        tc_fence_after();
+        const uint32_t st = smem_u32(tiles + (size_t)s * stage_bytes);
+        const uint32_t ahi = st, bhi = st + a_bytes;
+        const uint32_t alo = st + a_bytes + b_bytes, blo = st + 2 * a_bytes + b_bytes;
+#pragma unroll
+        for (int kk = 0; kk < kBK / kUmmaK; ++kk) {
+          const uint32_t off = (uint32_t)kk * kUmmaK * 2;
+          const uint32_t acc = (kt > 0 || kk > 0) ? 1u : 0u;
+          umma_bf16_pair(tmem, sw_desc(ahi + off), sw_desc(bhi + off), idesc, acc);
+          if (kSplit) {
+            umma_bf16_pair(tmem, sw_desc(ahi + off), sw_desc(blo + off), idesc, 1u);
+            umma_bf16_pair(tmem, sw_desc(alo + off), sw_desc(bhi + off), idesc, 1u);
+          }
+        }
+        umma_commit_pair(&sh->empty[s]);
+        ++done;
+      }
+      if (done == num_k) {
+        umma_commit_pair(&sh->tmem_full);
+      } else {
+        umma_commit_pair_local(&sh->drain);
+        mbar_wait_bounded(smem_u32(&sh->drain), 0, nullptr, kMbarWaitNs / 8);
+      }
+    }
+  } else {
+    // epilogue: warps 2..5 -> TMEM lane quarters 2, 3, 0, 1 of this CTA's rows
+    const int quarter = warp & 3;
+    const int m = m0 + quarter * 32 + lane;
+    const bool ok = __all_sync(0xffffffffu, mbar_wait<true>(&sh->tmem_full, 0, abort_flag, status));
+    tc_fence_after();
+    if (ok) {
+      for (int c = 0; c < BN; c += 16) {
+        float v[16];
+        tmem_ld16(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)c, v);
+        if (m < n) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int b = b0 + c + j;
+            if (b < p) {
+              float out = v[j];
+              if (shift != 0.f) out = fmaf(shift, __ldg(Vf + (int64_t)b * ldvf + m), out);
+              W[(int64_t)b * ldw + m] = out;
+            }
+          }
+        }
+      }
+    }
+  }
+  __syncwarp();
+  tc_fence_before();
+  // neither CTA releases its TMEM or shared memory while the pair's MMAs,
+  // copies or commits may still reach it
+  cluster_sync_all();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(tmem_cols)
+                 : "memory");
+  }
+}
+
+// ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
 
@@ -356,7 +572,10 @@ int launch_dense_tcgen05(const __nv_bfloat16 *A_hi, const __nv_bfloat16 *A_lo, i
   const int BN = (int)((pt + 15) / 16 * 16);
   uint32_t cols = 32;
   while ((int)cols < BN) cols <<= 1;
-  const uint32_t a_bytes = kBM * kBK * 2, b_bytes = (uint32_t)BN * kBK * 2;
+  // CTA pairs (2-SM MMAs, M = 256) once the operator spans several pair tiles
+  const bool pair = n >= kPairMinRows && BN >= 64 && BN % 32 == 0;
+  const uint32_t a_bytes = kBM * kBK * 2;
+  const uint32_t b_bytes = (uint32_t)(pair ? BN / 2 : BN) * kBK * 2;
   const uint32_t stage_bytes = (split ? 2u : 1u) * (a_bytes + b_bytes);
   const size_t budget = 200 * 1024;
   int stages = (int)(budget / stage_bytes);
@@ -365,14 +584,34 @@ int launch_dense_tcgen05(const __nv_bfloat16 *A_hi, const __nv_bfloat16 *A_lo, i
   const size_t smem = 1024 + (size_t)stages * stage_bytes + sizeof(GemmShared);
 
   CUtensorMap mahi, malo, mbhi, mblo;
+  const uint32_t b_rows = (uint32_t)(pair ? BN / 2 : BN);
   if (!make_map(&mahi, A_hi, n, n, lda, kBM)) return MFG_ERR_CUDA;
-  if (!make_map(&mbhi, V_hi, n, p, ldvb, (uint32_t)BN)) return MFG_ERR_CUDA;
+  if (!make_map(&mbhi, V_hi, n, p, ldvb, b_rows)) return MFG_ERR_CUDA;
   if (split) {
     if (!make_map(&malo, A_lo, n, n, lda, kBM)) return MFG_ERR_CUDA;
-    if (!make_map(&mblo, V_lo, n, p, ldvb, (uint32_t)BN)) return MFG_ERR_CUDA;
+    if (!make_map(&mblo, V_lo, n, p, ldvb, b_rows)) return MFG_ERR_CUDA;
   } else {
     malo = mahi;
     mblo = mbhi;
+  }
+  if (pair) {
+    // grid.x: two CTAs per 256-row tile (the cluster dimension)
+    dim3 grid((unsigned)(2 * ((n + 2 * kBM - 1) / (2 * kBM))), (unsigned)((p + BN - 1) / BN));
+    if (grid.y > 65535) return MFG_ERR_UNSUPPORTED;
+    if (split) {
+      MFG_CUDA_TRY(cudaFuncSetAttribute(dense_tcgen05_pair_kernel<true>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      dense_tcgen05_pair_kernel<true><<<grid, kGemmThreads, smem, s>>>(
+          mahi, malo, mbhi, mblo, Vf, ldvf, W, ldw, (int)n, (int)p, BN, stages, cols,
+          (float)shift, status);
+    } else {
+      MFG_CUDA_TRY(cudaFuncSetAttribute(dense_tcgen05_pair_kernel<false>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      dense_tcgen05_pair_kernel<false><<<grid, kGemmThreads, smem, s>>>(
+          mahi, malo, mbhi, mblo, Vf, ldvf, W, ldw, (int)n, (int)p, BN, stages, cols,
+          (float)shift, status);
+    }
+    return MFG_LAUNCH_STATUS();
   }
   dim3 grid((unsigned)((n + kBM - 1) / kBM), (unsigned)((p + BN - 1) / BN));
   if (grid.y > 65535) return MFG_ERR_UNSUPPORTED;
