@@ -316,7 +316,13 @@ def gpu_arm(args):
     return result, prob
 
 
-def roofline(prof, peaks, steps):
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from one ncu
+# capture of that exact launch: --set full on `--config rbf16k4` (the same operator and
+# panel as rbf16k), kernel dense_tcgen05_pair_kernel<1>: 1.107433 GB read + 3.28 MB written.
+TRAFFIC = {("rbf16k", "bf16x3", "operator apply"): 1.107433e9 + 3.27936e6}
+
+
+def roofline(prof, peaks, steps, config=None, precision=None):
     """The class with the largest time share; HBM- or tensor-bound by its class."""
     total = sum(v["ms"] for v in prof.values()) or 1.0
     shares = {c: v["ms"] / total for c, v in prof.items()}
@@ -340,7 +346,9 @@ def roofline(prof, peaks, steps):
         achieved = (fl / launches) / (apply_ms / 1e3 / launches) / 1e12
         peak = peaks["tensor_sustained"]
         return {"kernel": "operator apply", "bound": "tensor", "achieved": achieved, "peak": peak,
-                "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                "unit": "TFLOP/s", "frac": achieved / peak,
+                "traffic": TRAFFIC.get((config, precision, "operator apply")),
+                "traffic_unit": "bytes per launch",
                 "time_share": apply_ms / total, "launches": launches, "shares": shares}
     b = prof["apply"]["bytes"]
     achieved = (b / launches) / (apply_ms / 1e3 / launches) / 1e9
@@ -535,7 +543,7 @@ def main():
                     help="requests of the plain fp32 comparison (0: all of them)")
     ap.add_argument("--rate", type=float, default=150.0)
     ap.add_argument("--slots", type=int, default=8)
-    ap.add_argument("--inflight", type=int, default=2,
+    ap.add_argument("--inflight", type=int, default=3,
                     help="independent solves in flight (round-robin over CUDA streams)")
     ap.add_argument("--precision", default="bf16x3", choices=["fp32", "bf16", "bf16x3", "fp64"])
     ap.add_argument("--cpu-probes", type=int, default=8)
@@ -562,7 +570,7 @@ def main():
     world = res["world"]
     peaks = _peaks()
     value = world * args.steps / (res["total_ms"] / 1e3)
-    rl = roofline(res["prof"], peaks, args.steps)
+    rl = roofline(res["prof"], peaks, args.steps, args.config, args.precision)
     rl["peak_source"] = f"of {peaks['source']}"
     launches = res["launches"]
     step_ms = res["step_ms"]
