@@ -234,11 +234,79 @@ rbf_kernel(const float *__restrict__ x, int64_t n, int dim, double s2, double in
   }
 }
 
+// fp32 / bf16 / bf16 hi+lo entries.  A CTA covers kRbfRows rows x 2048
+// columns: the columns' points are staged in shared memory once (coalesced,
+// coordinate-major) and reused for every row; each thread forms eight
+// consecutive entries of a row and stores them with one 16-byte store per
+// bf16 array (two for fp32).  Each entry is computed exactly as in rbf_kernel.
+constexpr int kRbfRows = 16;
+constexpr int kRbfCols = 256 * 8;
+constexpr int kRbfMaxDim = 4;
+
+__global__ void __launch_bounds__(256)
+rbf8_kernel(const float *__restrict__ x, int64_t n, int dim, float s2, float inv2l2, int prec,
+            int dlogell, void *__restrict__ a, void *__restrict__ a_lo, int64_t lda) {
+  __shared__ __align__(16) float xs[kRbfMaxDim][kRbfCols];
+  const int64_t c0 = (int64_t)blockIdx.x * kRbfCols;
+  const int64_t r0 = (int64_t)blockIdx.y * kRbfRows;
+  for (int t = threadIdx.x; t < kRbfCols * dim; t += 256) {
+    const int c = t / dim, d = t - c * dim;  // x is point-major: coalesced reads
+    const int64_t j = c0 + c;
+    xs[d][c] = j < n ? x[j * dim + d] : 0.f;
+  }
+  __syncthreads();
+  const int64_t j0 = c0 + (int64_t)threadIdx.x * 8;
+  if (j0 >= lda) return;
+  for (int rr = 0; rr < kRbfRows; ++rr) {
+    const int64_t i = r0 + rr;
+    if (i >= n) return;
+    float v[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      float d2 = 0.f;
+      for (int d = 0; d < dim; ++d) {
+        const float df = x[i * dim + d] - xs[d][threadIdx.x * 8 + e];
+        d2 = fmaf(df, df, d2);
+      }
+      float w = s2 * expf(-d2 * inv2l2);
+      if (dlogell) w *= 2.f * d2 * inv2l2;
+      v[e] = (j0 + e < n) ? w : 0.f;
+    }
+    const int64_t o = i * lda + j0;  // 8-element aligned: lda % 8 == 0
+    if (prec == MFG_PREC_FP32) {
+      float4 *dst = reinterpret_cast<float4 *>(reinterpret_cast<float *>(a) + o);
+      dst[0] = make_float4(v[0], v[1], v[2], v[3]);
+      dst[1] = make_float4(v[4], v[5], v[6], v[7]);
+      continue;
+    }
+    uint32_t hw[4], lw[4];
+#pragma unroll
+    for (int e = 0; e < 8; e += 2) {
+      const __nv_bfloat16 h0 = __float2bfloat16_rn(v[e]), h1 = __float2bfloat16_rn(v[e + 1]);
+      hw[e / 2] = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
+      const __nv_bfloat16 l0 = __float2bfloat16_rn(v[e] - __bfloat162float(h0));
+      const __nv_bfloat16 l1 = __float2bfloat16_rn(v[e + 1] - __bfloat162float(h1));
+      lw[e / 2] = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
+    }
+    *reinterpret_cast<uint4 *>(reinterpret_cast<__nv_bfloat16 *>(a) + o) =
+        make_uint4(hw[0], hw[1], hw[2], hw[3]);
+    if (prec == MFG_PREC_BF16X3)
+      *reinterpret_cast<uint4 *>(reinterpret_cast<__nv_bfloat16 *>(a_lo) + o) =
+          make_uint4(lw[0], lw[1], lw[2], lw[3]);
+  }
+}
+
 int launch_rbf_build(const float *x, int64_t n, int dim, double s2, double ell, int precision,
                      int dlogell, void *a, void *a_lo, int64_t lda, cudaStream_t s) {
   if (n <= 0) return MFG_OK;
   if (n > 65535) return MFG_ERR_UNSUPPORTED;
   const double inv2l2 = 1.0 / (2.0 * ell * ell);
+  if (precision != MFG_PREC_FP64 && dim <= kRbfMaxDim && lda % 8 == 0 && ((uintptr_t)a & 15) == 0 &&
+      (a_lo == nullptr || ((uintptr_t)a_lo & 15) == 0)) {
+    rbf8_kernel<<<dim3((unsigned)ceil_div(lda, kRbfCols), (unsigned)ceil_div(n, kRbfRows)), 256, 0, s>>>(
+        x, n, dim, (float)s2, (float)inv2l2, precision, dlogell, a, a_lo, lda);
+    return MFG_LAUNCH_STATUS();
+  }
   rbf_kernel<<<dim3((unsigned)ceil_div(lda, 256), (unsigned)n), 256, 0, s>>>(
       x, n, dim, s2, inv2l2, precision, dlogell, a, a_lo, lda);
   return MFG_LAUNCH_STATUS();
