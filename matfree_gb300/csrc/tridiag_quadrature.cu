@@ -62,16 +62,29 @@ __global__ void tridiag_ql_kernel(int k, int64_t p, const double *__restrict__ H
       g = D_(m) - D_(l) + E_(l) / (g + copysign(r, g));
       double s = 1.0, c = 1.0, shift_acc = 0.0;
       bool deflated = false;
+      // The chase reads d_i, e_i, z_i before they are written in this sweep,
+      // and d_{i+1}, z_{i+1} as left by the previous rotation: those travel in
+      // registers and the next rotation's inputs are loaded one step ahead, so
+      // shared-memory latency stays off the float64 dependence chain.
+      double d_up = D_(m), z_up = Z_(m);                // d_{i+1}, z_{i+1}
+      double e_i = E_(m - 1), d_i = D_(m - 1), z_i = Z_(m - 1);
       for (int i = m - 1; i >= l; --i) {
-        const double f = s * E_(i);
-        const double bb = c * E_(i);
+        double e_nx = 0.0, d_nx = 0.0, z_nx = 0.0;
+        if (i > l) {
+          e_nx = E_(i - 1);
+          d_nx = D_(i - 1);
+          z_nx = Z_(i - 1);
+        }
+        const double f = s * e_i;
+        const double bb = c * e_i;
         // Entries of Lanczos tridiagonals are far from the overflow range, so
         // the rotation uses one reciprocal square root of f^2 + g^2 (in place
         // of hypot and a division): float64 issue slots are scarce on GB300.
         const double rr = fma(f, f, g * g);
         if (rr == 0.0) {  // split: recover and restart the sweep
           E_(i + 1) = 0.0;
-          D_(i + 1) -= shift_acc;
+          D_(i + 1) = d_up - shift_acc;
+          Z_(i + 1) = z_up;
           E_(m) = 0.0;
           deflated = true;
           break;
@@ -81,16 +94,20 @@ __global__ void tridiag_ql_kernel(int k, int64_t p, const double *__restrict__ H
         E_(i + 1) = r;
         s = f * rinv;
         c = g * rinv;
-        g = D_(i + 1) - shift_acc;
-        r = (D_(i) - g) * s + 2.0 * c * bb;
+        g = d_up - shift_acc;
+        r = (d_i - g) * s + 2.0 * c * bb;
         shift_acc = s * r;
         D_(i + 1) = g + shift_acc;
         g = c * r - bb;
-        const double zf = Z_(i + 1);
-        Z_(i + 1) = s * Z_(i) + c * zf;
-        Z_(i) = c * Z_(i) - s * zf;
+        Z_(i + 1) = s * z_i + c * z_up;
+        z_up = c * z_i - s * z_up;  // the new z_i, input of the next rotation
+        d_up = d_i;
+        e_i = e_nx;
+        d_i = d_nx;
+        z_i = z_nx;
       }
       if (deflated) continue;
+      Z_(l) = z_up;
       D_(l) -= shift_acc;
       E_(l) = g;
       E_(m) = 0.0;
