@@ -495,6 +495,72 @@ def grad_arm(args):
     print(json.dumps(line), flush=True)
 
 
+def gp_arm(args):
+    """GP log-pdf (SLQ log-det + CG solve) and d/dtheta, RBF n=8192, k=48, p=128, per step."""
+    import torch
+
+    import matfree_gb300 as mf
+
+    torch.cuda.set_device(0)
+    n, k, p, tol = 8192, 48, 128, 1e-5
+    rng = np.random.default_rng(0)
+    x = rng.uniform(0.0, 1.0, size=(n, 3)).astype(np.float32)
+    y = rng.standard_normal(n).astype(np.float32)
+    xd, yd = torch.from_numpy(x).cuda(), torch.from_numpy(y).cuda()
+    theta0 = np.array([0.0, math.log(0.2), math.log(1e-2)])
+    key = mf.prng.prng_key(1)
+    V = mf.stochtrace.sampler_signs(torch.ones(n, device="cuda"), num=p)(key)
+
+    def step():
+        th = torch.tensor(theta0, dtype=torch.float64, requires_grad=True)
+        val = mf.gp.rbf_logpdf(xd, th, yd, V, k, precision=args.precision, cg_tol=tol)
+        val.backward()
+        return val.detach(), th.grad
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        val, grad = step()
+    torch.cuda.synchronize()
+    secs = (time.perf_counter() - t0) / args.steps
+    op = mf.RBFKernelOperator.from_theta(xd, theta0, precision=args.precision)
+    _, its = mf.linalg.cg_batched(op, yd[None, :], tol=tol)
+    its = int(its[0])
+    # float64 oracle: log-det gradient on the first probes, CG for a bounded
+    # number of iterations, both extrapolated (probes; CG iterations)
+    from oracle import adjoint as oadj
+    from oracle import gp as ogp
+    from oracle import philox
+
+    num = args.cpu_probes
+    Vs = philox.rademacher(np.asarray(key, np.uint32), num, n)
+    t1 = time.perf_counter()
+    matmat, vjp_matmat = oadj.rbf_vjp_factory(x.astype(np.float64), theta0)
+    _, g_ref = oadj.slq_grad_batched(matmat, vjp_matmat, 3, k, Vs)
+    ld_s = time.perf_counter() - t1
+    K, _, _ = oadj.rbf_matrices(x.astype(np.float64), theta0)
+    cg_cap = min(its, 100)
+    t2 = time.perf_counter()
+    ogp.cg(lambda v: K @ v, y.astype(np.float64), tol=0.0, maxiter=cg_cap)
+    cg_s = (time.perf_counter() - t2) * its / max(cg_cap, 1)
+    cpu_s = ld_s * p / num + 2 * cg_s  # forward solve + the gradient's contractions reuse alpha
+    line = {"metric": "GP logpdf+grad solves/s", "value": 1.0 / secs, "unit": "solves/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": f"f32 basis / {args.precision} operator / f64 reductions",
+            "data": "synthetic (seeded)",
+            "config": {"workload": f"GP log-pdf (SLQ log-det + CG, tol {tol}) + d/dtheta, RBF n={n}, k={k}, "
+                                   f"p={p}, theta=(0, log 0.2, log 1e-2)", "cg_iterations": its},
+            "estimate": float(val), "grad": grad.tolist(),
+            "logdet_grad_vs_fp64_oracle": {"oracle": g_ref.tolist(), "on": f"first {num} probes"},
+            "cpu_baseline": {"value": 1.0 / cpu_s, "unit": "solves/s", "cores": len(os.sched_getaffinity(0)),
+                             "kind": "port",
+                             "sample": f"log-det gradient on {num} of {p} probes and {cg_cap} of {its} CG "
+                                       "iterations (float64 restatement), extrapolated linearly"}}
+    print(json.dumps(line), flush=True)
+
+
 def serve_arm(args):
     """Mixed request stream through the continuous-batching server vs one-by-one fp32."""
     import torch
@@ -537,7 +603,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="rbf16k", choices=sorted(CONFIGS) + ["serve", "grad8k"])
+    ap.add_argument("--config", default="rbf16k", choices=sorted(CONFIGS) + ["serve", "grad8k", "gp8k"])
     ap.add_argument("--requests", type=int, default=64)
     ap.add_argument("--baseline-requests", type=int, default=0,
                     help="requests of the plain fp32 comparison (0: all of them)")
@@ -557,6 +623,9 @@ def main():
         return
     if args.config == "grad8k" and args.impl == "ours":
         grad_arm(args)
+        return
+    if args.config == "gp8k" and args.impl == "ours":
+        gp_arm(args)
         return
     if args.impl == "reference":
         line = reference_arm(args)

@@ -194,6 +194,24 @@ MFG_API int mfg_rbf_build_dlogell(const float *x, int64_t n, int32_t dim, double
                                   int32_t precision, void *a, void *a_lo, int64_t lda, void *stream);
 
 /* Split a float32 matrix into bf16 hi = bf16(a) and lo = bf16(a - hi). */
+/* ---- conjugate gradients ------------------------------------------------ */
+
+/* Workspace bytes of mfg_cg for p right-hand sides (0 on bad arguments). */
+MFG_API size_t mfg_cg_workspace_bytes(const mfg_operator *op, int64_t p, int64_t ld);
+
+/* Solve (A + shift I) X = B for each of the p probe-major rows of B (ld
+ * elements apart) by conjugate gradients from X = 0 without preconditioner,
+ * as jax.scipy.sparse.linalg.cg (used by matfree's Gaussian log-pdf,
+ * tutorials/8_gaussian_logpdf.py:50): a row stops once ||r||^2 <=
+ * max(tol^2 ||b||^2, atol^2) or after maxiter iterations (maxiter <= 0:
+ * 10 n), and stays unchanged while the other rows iterate.  iters (device,
+ * p int32, may be NULL) receives the iterations each row ran.  Synchronises
+ * `stream` once per iteration (to test whether any row still runs); returns
+ * the first device-side error status (e.g. MFG_ERR_TIMEOUT) or MFG_OK. */
+MFG_API int mfg_cg(const mfg_operator *op, int64_t p, const void *B, void *X, int64_t ld,
+                   double tol, double atol, int64_t maxiter, int32_t *iters, void *workspace,
+                   size_t workspace_bytes, void *stream);
+
 /* ---- launch accounting (diagnostics) ------------------------------------ */
 enum {
   MFG_PROF_APPLY = 0,  /* operator application (GEMM / SpMM / callback)        */

@@ -7,12 +7,12 @@ operator applied to all probes at once by CUDA kernels in
 ``libmatfree_gb300.so`` (C ABI: include/matfree_gb300.h).
 """
 
-from . import decomp, funm, operators, prng, stochtrace, tree  # noqa: F401
+from . import decomp, funm, gp, linalg, operators, prng, stochtrace, tree  # noqa: F401
 from ._lib import library_path, lib  # noqa: F401
 from .operators import CallbackOperator, CSROperator, DenseOperator, RBFKernelOperator  # noqa: F401
 
 __all__ = [
-    "decomp", "funm", "stochtrace", "prng", "operators", "tree",
+    "decomp", "funm", "stochtrace", "prng", "operators", "tree", "linalg", "gp",
     "DenseOperator", "RBFKernelOperator", "CSROperator", "CallbackOperator",
     "lib", "library_path",
 ]

@@ -481,6 +481,94 @@ static int launch_square(const double *x, double *y, int64_t p, cudaStream_t s) 
 
 using namespace mfg;
 
+// ---------------------------------------------------------------------------
+// Conjugate gradients (jax.scipy.sparse.linalg.cg with x0 = 0 and no
+// preconditioner, one independent solve per probe row of the panel)
+// ---------------------------------------------------------------------------
+
+struct CgLayout {
+  size_t r, p, w, hi, lo, rs0, rs1, pap, thr, partials, counters, nactive, status, iters, total;
+};
+
+static CgLayout cg_layout(const mfg_operator *op, int64_t p, int64_t ld) {
+  CgLayout L{};
+  const size_t es = (size_t)elem_size_for(op);
+  const int64_t nch = es == 8 ? max_fused_chunks<double>(op->n) : max_fused_chunks<float>(op->n);
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    const size_t o = off;
+    off = align_up(off + bytes, 256);
+    return o;
+  };
+  L.r = take((size_t)p * ld * es);
+  L.p = take((size_t)p * ld * es);
+  L.w = take((size_t)p * ld * es);
+  L.hi = take(uses_bf16(op) ? (size_t)p * ld * 2 : 0);
+  L.lo = take(uses_bf16(op) && op->precision == MFG_PREC_BF16X3 ? (size_t)p * ld * 2 : 0);
+  L.rs0 = take((size_t)p * 8);
+  L.rs1 = take((size_t)p * 8);
+  L.pap = take((size_t)p * 8);
+  L.thr = take((size_t)p * 8);
+  L.partials = take((size_t)p * nch * 8);
+  L.counters = take((size_t)p * 4);
+  L.nactive = take(16);
+  L.status = take(16);
+  L.iters = take((size_t)p * 4);
+  L.total = off + 256;
+  return L;
+}
+
+template <typename T>
+static int run_cg(const mfg_operator *op, int64_t p, const T *B, T *X, int64_t ld, double tol,
+                  double atol, int64_t maxiter, int32_t *iters_out, const CgLayout &L, char *ws,
+                  cudaStream_t s) {
+  const int64_t n = op->n;
+  T *R = reinterpret_cast<T *>(ws + L.r);
+  T *P = reinterpret_cast<T *>(ws + L.p);
+  T *W = reinterpret_cast<T *>(ws + L.w);
+  __nv_bfloat16 *hi = uses_bf16(op) ? reinterpret_cast<__nv_bfloat16 *>(ws + L.hi) : nullptr;
+  __nv_bfloat16 *lo = (uses_bf16(op) && op->precision == MFG_PREC_BF16X3)
+                          ? reinterpret_cast<__nv_bfloat16 *>(ws + L.lo)
+                          : nullptr;
+  double *rs[2] = {reinterpret_cast<double *>(ws + L.rs0), reinterpret_cast<double *>(ws + L.rs1)};
+  double *pap = reinterpret_cast<double *>(ws + L.pap);
+  double *thr = reinterpret_cast<double *>(ws + L.thr);
+  double *partials = reinterpret_cast<double *>(ws + L.partials);
+  unsigned *counters = reinterpret_cast<unsigned *>(ws + L.counters);
+  int *nactive = reinterpret_cast<int *>(ws + L.nactive);
+  int *status = reinterpret_cast<int *>(ws + L.status);
+  int *iters = iters_out ? iters_out : reinterpret_cast<int *>(ws + L.iters);
+  const double vecb = (double)n * (double)p * (double)sizeof(T);
+  double ab = 0.0, af = 0.0;
+  apply_cost(op, p, &ab, &af);
+
+  MFG_CUDA_TRY(cudaMemsetAsync(counters, 0, (size_t)p * 4, s));
+  MFG_CUDA_TRY(cudaMemsetAsync(status, 0, 16, s));
+  MFG_LAUNCH(MFG_PROF_OTHER, 4.0 * vecb, 2.0 * vecb / sizeof(T),
+             launch_cg_init<T>(B, X, R, P, ld, n, p, hi, lo, partials, counters, tol * tol,
+                               atol * atol, rs[0], thr, iters, s));
+  for (int64_t it = 0; it < maxiter; ++it) {
+    double *rc = rs[it & 1], *rn = rs[(it + 1) & 1];
+    MFG_CUDA_TRY(cudaMemsetAsync(nactive, 0, sizeof(int), s));
+    MFG_LAUNCH(MFG_PROF_APPLY, ab, af, apply_op<T>(op, P, ld, W, ld, p, hi, lo, ld, nullptr, status, s));
+    MFG_LAUNCH(MFG_PROF_PROJ, 2.0 * vecb, 2.0 * vecb / sizeof(T),
+               launch_proj<T>(P, ld, ld, 1, W, ld, n, p, partials, counters, pap, 1, 1, s, status));
+    MFG_LAUNCH(MFG_PROF_SUB, 6.0 * vecb, 6.0 * vecb / sizeof(T),
+               launch_cg_update<T>(X, R, P, W, ld, n, p, rc, pap, thr, partials, counters, rn,
+                                   nactive, iters, s));
+    MFG_LAUNCH(MFG_PROF_SCALE, 3.0 * vecb, 2.0 * vecb / sizeof(T),
+               launch_cg_direction<T>(P, R, ld, n, p, rc, rn, thr, hi, lo, s));
+    int host_active = 0;
+    MFG_CUDA_TRY(cudaMemcpyAsync(&host_active, nactive, sizeof(int), cudaMemcpyDeviceToHost, s));
+    MFG_CUDA_TRY(cudaStreamSynchronize(s));
+    if (host_active == 0) break;
+  }
+  int host_status = 0;
+  MFG_CUDA_TRY(cudaMemcpyAsync(&host_status, status, sizeof(int), cudaMemcpyDeviceToHost, s));
+  MFG_CUDA_TRY(cudaStreamSynchronize(s));
+  return host_status;
+}
+
 extern "C" {
 
 int mfg_version(void) { return 100; }
@@ -755,6 +843,28 @@ int mfg_slq(const mfg_operator *op, int64_t k, int64_t p, const void *probes, in
                                        reinterpret_cast<double *>(ws + L.fsq), status, s));
   if (mean_sem) MFG_LAUNCH(MFG_PROF_QUAD, 8.0 * p, 3.0 * p, launch_mean_sem(values, p, mean_sem, s));
   return MFG_OK;
+}
+
+size_t mfg_cg_workspace_bytes(const mfg_operator *op, int64_t p, int64_t ld) {
+  if (check_op(op) != MFG_OK || p <= 0 || ld < op->n) return 0;
+  return cg_layout(op, p, ld).total;
+}
+
+int mfg_cg(const mfg_operator *op, int64_t p, const void *B, void *X, int64_t ld, double tol,
+           double atol, int64_t maxiter, int32_t *iters, void *workspace, size_t workspace_bytes,
+           void *stream) {
+  MFG_TRY(check_op(op));
+  MFG_TRY(check_panel(op, p, ld));
+  if (!B || !X || !aligned16(B) || !aligned16(X) || tol < 0.0 || atol < 0.0) return MFG_ERR_BAD_ARG;
+  if (op->kind == MFG_OP_CALLBACK && op->shift != 0.0) return MFG_ERR_UNSUPPORTED;
+  const CgLayout L = cg_layout(op, p, ld);
+  if (!workspace || workspace_bytes < L.total) return MFG_ERR_WORKSPACE;
+  char *ws = ws_base(workspace);
+  cudaStream_t s = as_stream(stream);
+  if (maxiter <= 0) maxiter = 10 * op->n;  // jax.scipy.sparse.linalg.cg's default
+  if (op->precision == MFG_PREC_FP64)
+    return run_cg<double>(op, p, (const double *)B, (double *)X, ld, tol, atol, maxiter, iters, L, ws, s);
+  return run_cg<float>(op, p, (const float *)B, (float *)X, ld, tol, atol, maxiter, iters, L, ws, s);
 }
 
 static int rbf_build(const float *x, int64_t n, int32_t dim, double s2, double ell,

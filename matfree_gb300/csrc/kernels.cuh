@@ -33,6 +33,19 @@ int launch_scale(const T *Win, int64_t w_bstride, int64_t n, int64_t p, const do
                  int64_t out_bstride, __nv_bfloat16 *hi, __nv_bfloat16 *lo, int64_t bf_bstride,
                  cudaStream_t s);
 int launch_inv(const double *x, double *y, int64_t p, cudaStream_t s);
+// conjugate gradients on probe-major panels (lanczos_kernels.cu)
+template <typename T>
+int launch_cg_init(const T *B, T *X, T *R, T *P, int64_t ld, int64_t n, int64_t p,
+                   __nv_bfloat16 *hi, __nv_bfloat16 *lo, double *partials, unsigned *counters,
+                   double tol2, double atol2, double *rs, double *thr, int *iters, cudaStream_t s);
+template <typename T>
+int launch_cg_update(T *X, T *R, const T *P, const T *W, int64_t ld, int64_t n, int64_t p,
+                     const double *rs, const double *pap, const double *thr, double *partials,
+                     unsigned *counters, double *rs_next, int *nactive, int *iters, cudaStream_t s);
+template <typename T>
+int launch_cg_direction(T *P, const T *R, int64_t ld, int64_t n, int64_t p, const double *rs,
+                        const double *rs_next, const double *thr, __nv_bfloat16 *hi,
+                        __nv_bfloat16 *lo, cudaStream_t s);
 
 // adjoint_kernels.cu
 int launch_pi_gamma(const double *H, const double *dH, const double *dc, const double *c, int k,

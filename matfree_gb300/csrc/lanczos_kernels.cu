@@ -996,7 +996,205 @@ int launch_inv(const double *x, double *y, int64_t p, cudaStream_t s) {
   return MFG_LAUNCH_STATUS();
 }
 
+// ---------------------------------------------------------------------------
+// Conjugate gradients, one independent CG per probe row of a panel (as
+// jax.scipy.sparse.linalg.cg under vmap: a finished probe stays frozen while
+// the others iterate).  The vector updates of an iteration carry the float64
+// squared norm of the new residual, summed across CTAs in chunk order.
+// ---------------------------------------------------------------------------
+
+// CTA sum of a per-thread float64 value, then the cross-CTA sum of probe b
+// in chunk order by the last CTA to arrive; returns true (with *total) in
+// that CTA's thread 0.
+__device__ __forceinline__ bool probe_sum(double v, int64_t b, int64_t c, int nchunks,
+                                          double *partials, unsigned *counters, double *total) {
+  __shared__ double red[kWarps];
+  v = warp_sum(v);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int q = 0; q < kWarps; ++q) t += red[q];
+    if (nchunks == 1) {
+      *total = t;
+      return true;
+    }
+    partials[b * nchunks + c] = t;
+  }
+  if (nchunks == 1) return false;
+  if (!arrive_last(counters, b, nchunks)) return false;
+  if (threadIdx.x != 0) return false;
+  t = 0.0;
+  for (int q = 0; q < nchunks; ++q) t += __ldcg(&partials[b * nchunks + q]);
+  counters[b] = 0u;
+  *total = t;
+  return true;
+}
+
+template <typename T>
+__device__ __forceinline__ void store_split(const T (&w)[kVPT][Vec<T>::width], int64_t n, int64_t c,
+                                            __nv_bfloat16 *hi, __nv_bfloat16 *lo) {
+  constexpr int W = Vec<T>::width;
+#pragma unroll
+  for (int e = 0; e < kVPT; ++e) {
+    const int64_t r = c * chunk_rows<T>() + ((int64_t)e * kThreads + threadIdx.x) * W;
+    if (r >= n) continue;
+#pragma unroll
+    for (int u = 0; u < W; ++u) {
+      const float x = (float)w[e][u];
+      const __nv_bfloat16 h = __float2bfloat16_rn(x);
+      hi[r + u] = h;
+      if (lo) lo[r + u] = __float2bfloat16_rn(x - __bfloat162float(h));
+    }
+  }
+}
+
+// X = 0, R = P = B, rs = ||B||^2, thr = max(tol^2 ||B||^2, atol^2)
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+cg_init_kernel(const T *__restrict__ B, T *__restrict__ X, T *__restrict__ R, T *__restrict__ P,
+               int64_t ld, int64_t n, __nv_bfloat16 *hi, __nv_bfloat16 *lo, int nchunks,
+               double *partials, unsigned *counters, double tol2, double atol2,
+               double *__restrict__ rs, double *__restrict__ thr, int *__restrict__ iters) {
+  constexpr int W = Vec<T>::width;
+  const int64_t c = blockIdx.x, b = blockIdx.y;
+  T w[kVPT][W], z[kVPT][W];
+  load_chunk<T>(B + b * ld, n, c, w);
+  double acc = 0.0;
+#pragma unroll
+  for (int e = 0; e < kVPT; ++e)
+#pragma unroll
+    for (int u = 0; u < W; ++u) {
+      acc = fma((double)w[e][u], (double)w[e][u], acc);
+      z[e][u] = (T)0;
+    }
+  store_chunk<T>(X + b * ld, n, c, z);
+  store_chunk<T>(R + b * ld, n, c, w);
+  store_chunk<T>(P + b * ld, n, c, w);
+  if (hi) store_split<T>(w, n, c, hi + b * ld, lo ? lo + b * ld : nullptr);
+  double t;
+  if (probe_sum(acc, b, c, nchunks, partials, counters, &t)) {
+    rs[b] = t;
+    thr[b] = fmax(tol2 * t, atol2);
+    if (iters) iters[b] = 0;
+  }
+}
+
+// For a probe still running (rs > thr): alpha = rs / pAp, X += alpha P,
+// R -= alpha W; every probe: rs_next = ||R||^2.  The last CTA of a probe
+// counts it into *nactive when it keeps running after this iteration.
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+cg_update_kernel(T *__restrict__ X, T *__restrict__ R, const T *__restrict__ P,
+                 const T *__restrict__ W, int64_t ld, int64_t n, const double *__restrict__ rs,
+                 const double *__restrict__ pap, const double *__restrict__ thr, int nchunks,
+                 double *partials, unsigned *counters, double *__restrict__ rs_next,
+                 int *__restrict__ nactive, int *__restrict__ iters) {
+  constexpr int VW = Vec<T>::width;
+  const int64_t c = blockIdx.x, b = blockIdx.y;
+  const bool active = rs[b] > thr[b];
+  T r[kVPT][VW];
+  load_chunk<T, false>(R + b * ld, n, c, r);
+  if (active) {
+    const T alpha = (T)(rs[b] / pap[b]);
+    T x[kVPT][VW], pv[kVPT][VW], wv[kVPT][VW];
+    load_chunk<T, false>(X + b * ld, n, c, x);
+    load_chunk<T>(P + b * ld, n, c, pv);
+    load_chunk<T>(W + b * ld, n, c, wv);
+#pragma unroll
+    for (int e = 0; e < kVPT; ++e)
+#pragma unroll
+      for (int u = 0; u < VW; ++u) {
+        x[e][u] = fma(alpha, pv[e][u], x[e][u]);
+        r[e][u] = fma(-alpha, wv[e][u], r[e][u]);
+      }
+    store_chunk<T>(X + b * ld, n, c, x);
+    store_chunk<T>(R + b * ld, n, c, r);
+  }
+  double acc = 0.0;
+#pragma unroll
+  for (int e = 0; e < kVPT; ++e)
+#pragma unroll
+    for (int u = 0; u < VW; ++u) acc = fma((double)r[e][u], (double)r[e][u], acc);
+  double t;
+  if (probe_sum(acc, b, c, nchunks, partials, counters, &t)) {
+    rs_next[b] = t;
+    if (active) {
+      if (iters) iters[b] += 1;
+      if (t > thr[b]) atomicAdd(nactive, 1);
+    }
+  }
+}
+
+// For a probe that ran this iteration: P = R + (rs_next / rs) P (and its
+// bf16 hi / lo copies for the tensor-core operator).
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+cg_direction_kernel(T *__restrict__ P, const T *__restrict__ R, int64_t ld, int64_t n,
+                    const double *__restrict__ rs, const double *__restrict__ rs_next,
+                    const double *__restrict__ thr, __nv_bfloat16 *hi, __nv_bfloat16 *lo) {
+  constexpr int VW = Vec<T>::width;
+  const int64_t c = blockIdx.x, b = blockIdx.y;
+  if (!(rs[b] > thr[b])) return;
+  const T beta = (T)(rs_next[b] / rs[b]);
+  T pv[kVPT][VW], r[kVPT][VW];
+  load_chunk<T, false>(P + b * ld, n, c, pv);
+  load_chunk<T>(R + b * ld, n, c, r);
+#pragma unroll
+  for (int e = 0; e < kVPT; ++e)
+#pragma unroll
+    for (int u = 0; u < VW; ++u) pv[e][u] = fma(beta, pv[e][u], r[e][u]);
+  store_chunk<T>(P + b * ld, n, c, pv);
+  if (hi) store_split<T>(pv, n, c, hi + b * ld, lo ? lo + b * ld : nullptr);
+}
+
+template <typename T>
+int launch_cg_init(const T *B, T *X, T *R, T *P, int64_t ld, int64_t n, int64_t p,
+                   __nv_bfloat16 *hi, __nv_bfloat16 *lo, double *partials, unsigned *counters,
+                   double tol2, double atol2, double *rs, double *thr, int *iters, cudaStream_t s) {
+  if (p <= 0 || n <= 0) return MFG_OK;
+  if (p > 65535) return MFG_ERR_UNSUPPORTED;
+  const int64_t nch = num_chunks<T>(n);
+  cg_init_kernel<T><<<dim3((unsigned)nch, (unsigned)p), kThreads, 0, s>>>(
+      B, X, R, P, ld, n, hi, lo, (int)nch, partials, counters, tol2, atol2, rs, thr, iters);
+  return MFG_LAUNCH_STATUS();
+}
+
+template <typename T>
+int launch_cg_update(T *X, T *R, const T *P, const T *W, int64_t ld, int64_t n, int64_t p,
+                     const double *rs, const double *pap, const double *thr, double *partials,
+                     unsigned *counters, double *rs_next, int *nactive, int *iters, cudaStream_t s) {
+  if (p <= 0 || n <= 0) return MFG_OK;
+  if (p > 65535) return MFG_ERR_UNSUPPORTED;
+  const int64_t nch = num_chunks<T>(n);
+  cg_update_kernel<T><<<dim3((unsigned)nch, (unsigned)p), kThreads, 0, s>>>(
+      X, R, P, W, ld, n, rs, pap, thr, (int)nch, partials, counters, rs_next, nactive, iters);
+  return MFG_LAUNCH_STATUS();
+}
+
+template <typename T>
+int launch_cg_direction(T *P, const T *R, int64_t ld, int64_t n, int64_t p, const double *rs,
+                        const double *rs_next, const double *thr, __nv_bfloat16 *hi,
+                        __nv_bfloat16 *lo, cudaStream_t s) {
+  if (p <= 0 || n <= 0) return MFG_OK;
+  if (p > 65535) return MFG_ERR_UNSUPPORTED;
+  const int64_t nch = num_chunks<T>(n);
+  cg_direction_kernel<T><<<dim3((unsigned)nch, (unsigned)p), kThreads, 0, s>>>(
+      P, R, ld, n, rs, rs_next, thr, hi, lo);
+  return MFG_LAUNCH_STATUS();
+}
+
 #define MFG_INST(T)                                                                          \
+  template int launch_cg_init<T>(const T *, T *, T *, T *, int64_t, int64_t, int64_t,         \
+                                 __nv_bfloat16 *, __nv_bfloat16 *, double *, unsigned *,      \
+                                 double, double, double *, double *, int *, cudaStream_t);    \
+  template int launch_cg_update<T>(T *, T *, const T *, const T *, int64_t, int64_t, int64_t,  \
+                                   const double *, const double *, const double *, double *,  \
+                                   unsigned *, double *, int *, int *, cudaStream_t);         \
+  template int launch_cg_direction<T>(T *, const T *, int64_t, int64_t, int64_t,              \
+                                      const double *, const double *, const double *,         \
+                                      __nv_bfloat16 *, __nv_bfloat16 *, cudaStream_t);        \
   template int sub_proj_rows_per_thread<T>(int);                                               \
   template int64_t max_fused_chunks<T>(int64_t);                                               \
   template int launch_sub_proj<T>(const T *, int64_t, int64_t, int, const double *, int64_t,   \
