@@ -194,6 +194,34 @@ MFG_API int mfg_rbf_build_dlogell(const float *x, int64_t n, int32_t dim, double
                                   int32_t precision, void *a, void *a_lo, int64_t lda, void *stream);
 
 /* Split a float32 matrix into bf16 hi = bf16(a) and lo = bf16(a - hi). */
+/* ---- Golub-Kahan bidiagonalisation and product quadrature --------------- */
+
+/* Workspace bytes of mfg_bidiag / mfg_slq_product (0 on bad arguments). */
+MFG_API size_t mfg_bidiag_workspace_bytes(const mfg_operator *A, const mfg_operator *At, int64_t k,
+                                          int64_t p, int64_t ld);
+
+/* decomp.bidiag(k, reortho="full") (matfree/decomp.py:641-750) from every
+ * probe-major row of V0: A V ~ U B, A^T U = V B^T + residual e_k^T, with the
+ * operator A and its transpose At (both n x n; pad rectangular maps with
+ * zeros).  U, V: (p, k, ld) left / right vectors; alphas, betas: (p, k)
+ * float64 with B = diag(alphas) + superdiag(betas[:, 1:]) and betas[:, 0] =
+ * 0; residual (p, ld) = beta_k v_k; init_len_inv (p) = 1 / ||v0||.  Every
+ * vector is reorthogonalised twice (classical Gram-Schmidt) against the
+ * vectors of its side.  residual and init_len_inv may be NULL. */
+MFG_API int mfg_bidiag(const mfg_operator *A, const mfg_operator *At, int64_t k, int64_t p,
+                       const void *V0, int64_t ld, void *U, void *V, double *alphas,
+                       double *betas, void *residual, double *init_len_inv, void *workspace,
+                       size_t workspace_bytes, void *stream);
+
+/* funm.monte_carlo_funm_product(dense_funm_product_svd(f), bidiag(k))
+ * (matfree/funm.py:246-320) on every probe row: values[b] = ||v_b||^2
+ * e1^T f(B_b^T B_b) e1 with f = log (product log-determinant) or x ** param
+ * (Schatten norms: param = power / 2); mean_sem (2 doubles, may be NULL). */
+MFG_API int mfg_slq_product(const mfg_operator *A, const mfg_operator *At, int64_t k, int64_t p,
+                            const void *probes, int64_t ld, int32_t fun, double param,
+                            double *values, double *mean_sem, void *workspace,
+                            size_t workspace_bytes, void *stream);
+
 /* ---- conjugate gradients ------------------------------------------------ */
 
 /* Workspace bytes of mfg_cg for p right-hand sides (0 on bad arguments). */

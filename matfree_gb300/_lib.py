@@ -66,6 +66,11 @@ SIGNATURES = {
     "mfg_rbf_build_dlogell": (c_int, [c_void_p, c_int64, c_int32, c_double, c_double, c_int32, c_void_p, c_void_p, c_int64, c_void_p]),
     "mfg_split_bf16": (c_int, [c_void_p, c_int64, c_int64, c_int64, c_void_p, c_void_p, c_int64, c_void_p]),
     "mfg_cg_workspace_bytes": (c_size_t, [POINTER(MfgOperator), c_int64, c_int64]),
+    "mfg_bidiag_workspace_bytes": (c_size_t, [POINTER(MfgOperator), POINTER(MfgOperator), c_int64, c_int64, c_int64]),
+    "mfg_bidiag": (c_int, [POINTER(MfgOperator), POINTER(MfgOperator), c_int64, c_int64, c_void_p, c_int64, c_void_p,
+                           c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
+    "mfg_slq_product": (c_int, [POINTER(MfgOperator), POINTER(MfgOperator), c_int64, c_int64, c_void_p, c_int64,
+                                c_int32, c_double, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
     "mfg_cg": (c_int, [POINTER(MfgOperator), c_int64, c_void_p, c_void_p, c_int64, c_double, c_double, c_int64,
                        c_void_p, c_void_p, c_size_t, c_void_p]),
     "mfg_adjoint_workspace_bytes": (c_size_t, [POINTER(MfgOperator), c_int64, c_int64, c_int64]),

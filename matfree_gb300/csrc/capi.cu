@@ -482,6 +482,166 @@ static int launch_square(const double *x, double *y, int64_t p, cudaStream_t s) 
 using namespace mfg;
 
 // ---------------------------------------------------------------------------
+// Golub-Kahan bidiagonalisation with full reorthogonalisation
+// (matfree/decomp.py:608-750), batched over the probe rows of a panel, and
+// the product quadrature e1^T f(B^T B) e1 (matfree/funm.py:246-303)
+// ---------------------------------------------------------------------------
+
+struct BidiagLayout {
+  WsLayout base;  // working panel, norms, projections, partials, bf16 copies
+  size_t u, v, alphas, betas, gram, values, total;
+};
+
+static BidiagLayout bidiag_layout(const mfg_operator *A, const mfg_operator *At, int64_t k,
+                                  int64_t p, int64_t ld) {
+  BidiagLayout L{};
+  // bf16 copies of the panel when either operator runs on the tensor cores
+  const mfg_operator *big = uses_bf16(At) && !uses_bf16(A) ? At : A;
+  if (uses_bf16(At) && At->precision == MFG_PREC_BF16X3) big = At;
+  L.base = layout(big, k, p, ld);
+  const size_t es = (size_t)elem_size_for(A);
+  const int64_t kk = k > 0 ? k : 1;
+  size_t off = L.base.total;
+  auto take = [&](size_t bytes) {
+    const size_t o = off;
+    off = align_up(off + bytes, 256);
+    return o;
+  };
+  L.u = take((size_t)p * kk * ld * es);
+  L.v = take((size_t)p * kk * ld * es);
+  L.alphas = take((size_t)p * kk * 8);
+  L.betas = take((size_t)p * kk * 8);
+  L.gram = take((size_t)p * kk * kk * 8);
+  L.values = take((size_t)p * 8);
+  L.total = off + 256;
+  return L;
+}
+
+// H_b = B_b^T B_b for the upper bidiagonal B_b (alphas on the diagonal,
+// betas[1:] above it): diagonal a_i^2 + b_i^2 (b_0 = 0), off-diagonal a_i b_{i+1}
+__global__ void bidiag_gram_kernel(const double *__restrict__ alphas, const double *__restrict__ betas,
+                                   int64_t k, int64_t p, double *__restrict__ H) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= p * k) return;
+  const int64_t b = t / k, i = t - b * k;
+  const double a = alphas[b * k + i];
+  const double bi = i > 0 ? betas[b * k + i] : 0.0;
+  double *Hb = H + b * k * k;
+  Hb[i * k + i] = a * a + bi * bi;
+  if (i + 1 < k) {
+    const double o = a * betas[b * k + i + 1];
+    Hb[i * k + i + 1] = o;
+    Hb[(i + 1) * k + i] = o;
+  }
+}
+
+template <typename T>
+static int run_bidiag(const mfg_operator *A, const mfg_operator *At, int64_t k, int64_t p,
+                      const T *V0, int64_t ld, T *U, T *Vb, double *alphas, double *betas, T *R,
+                      double *init_len_inv, const BidiagLayout &BL, char *ws, cudaStream_t s) {
+  const WsLayout &L = BL.base;
+  const int64_t n = A->n;
+  const int64_t qb = k * ld;  // probe stride of the bases
+  const double vecb = (double)n * (double)p * (double)sizeof(T);
+  double ab = 0.0, af = 0.0, tb = 0.0, tf = 0.0;
+  apply_cost(A, p, &ab, &af);
+  apply_cost(At, p, &tb, &tf);
+  T *Wb = reinterpret_cast<T *>(ws + L.w);
+  T *panel = reinterpret_cast<T *>(ws + L.panel);
+  double *norm = reinterpret_cast<double *>(ws + L.norm);
+  double *len0 = reinterpret_cast<double *>(ws + L.len0);
+  double *h1 = reinterpret_cast<double *>(ws + L.h);
+  double *h2 = reinterpret_cast<double *>(ws + L.h2);
+  double *partials = reinterpret_cast<double *>(ws + L.partials);
+  unsigned *counters = reinterpret_cast<unsigned *>(ws + L.counters);
+  int *status = reinterpret_cast<int *>(ws + L.status);
+  const bool bf = uses_bf16(A) || uses_bf16(At);
+  const bool bflo = (uses_bf16(A) && A->precision == MFG_PREC_BF16X3) ||
+                    (uses_bf16(At) && At->precision == MFG_PREC_BF16X3);
+  __nv_bfloat16 *hi = bf ? reinterpret_cast<__nv_bfloat16 *>(ws + L.hi) : nullptr;
+  __nv_bfloat16 *lo = bflo ? reinterpret_cast<__nv_bfloat16 *>(ws + L.lo) : nullptr;
+  const __nv_bfloat16 *hiA = uses_bf16(A) ? hi : nullptr;
+  const __nv_bfloat16 *loA = uses_bf16(A) && A->precision == MFG_PREC_BF16X3 ? lo : nullptr;
+  const __nv_bfloat16 *hiT = uses_bf16(At) ? hi : nullptr;
+  const __nv_bfloat16 *loT = uses_bf16(At) && At->precision == MFG_PREC_BF16X3 ? lo : nullptr;
+
+  MFG_CUDA_TRY(cudaMemsetAsync(counters, 0, (size_t)p * 4, s));
+  MFG_CUDA_TRY(cudaMemsetAsync(status, 0, 16, s));
+  if (k > 0) {
+    MFG_CUDA_TRY(cudaMemsetAsync(alphas, 0, (size_t)p * k * 8, s));
+    MFG_CUDA_TRY(cudaMemsetAsync(betas, 0, (size_t)p * k * 8, s));
+  }
+  // ||v0|| (decomp.py:683) -> 1 / length; v_0 = v0 / ||v0||
+  MFG_LAUNCH(MFG_PROF_OTHER, vecb, 2.0 * vecb / sizeof(T),
+             launch_sub<T>(nullptr, 0, 0, 0, nullptr, 0, 0, V0, nullptr, ld, n, p, true, false,
+                           partials, counters, len0, nullptr, 0, s));
+  if (init_len_inv) MFG_LAUNCH(MFG_PROF_OTHER, 16.0 * p, (double)p, launch_inv(len0, init_len_inv, p, s));
+  if (k == 0) {
+    if (R) MFG_CUDA_TRY(cudaMemsetAsync(R, 0, (size_t)p * ld * sizeof(T), s));
+    return MFG_OK;
+  }
+  MFG_LAUNCH(MFG_PROF_SCALE, 2.0 * vecb, vecb / sizeof(T),
+             launch_scale<T>(V0, ld, n, p, len0, Vb, qb, hi, lo, ld, s));
+
+  // CGS2 of the working panel against `ncols` basis rows, then ||w|| into
+  // norm (and out2[b * o2s] when given), as in decomp.py:703-719
+  auto cgs2 = [&](const T *Q, int ncols, double *out2, int64_t o2s) -> int {
+    if (ncols == 0)
+      return launch_sub<T>(nullptr, 0, 0, 0, nullptr, 0, 0, Wb, Wb, ld, n, p, true, false, partials,
+                           counters, norm, out2, o2s, s, status);
+    const double pb = (ncols + 1.0) * vecb, pf = 2.0 * ncols * vecb / sizeof(T);
+    const double ub = (ncols + 2.0) * vecb;
+    MFG_LAUNCH(MFG_PROF_PROJ, pb, pf,
+               launch_proj<T>(Q, qb, ld, ncols, Wb, ld, n, p, partials, counters, h1, k, 1, s, status));
+    if (sub_proj_rows_per_thread<T>(ncols) > 0) {
+      MFG_LAUNCH(MFG_PROF_SUBPROJ, (ncols + 2.0) * vecb, 2.0 * pf,
+                 launch_sub_proj<T>(Q, qb, ld, ncols, h1, k, 1, Wb, ld, n, p, partials, counters, h2,
+                                    k, status, s));
+    } else {
+      MFG_LAUNCH(MFG_PROF_SUB, ub, pf,
+                 launch_sub<T>(Q, qb, ld, ncols, h1, k, 1, Wb, Wb, ld, n, p, false, true, partials,
+                               counters, norm, nullptr, 0, s, status));
+      MFG_LAUNCH(MFG_PROF_PROJ, pb, pf,
+                 launch_proj<T>(Q, qb, ld, ncols, Wb, ld, n, p, partials, counters, h2, k, 1, s,
+                                status));
+    }
+    MFG_LAUNCH(MFG_PROF_SUB, ub, pf + 2.0 * vecb / sizeof(T),
+               launch_sub<T>(Q, qb, ld, ncols, h2, k, 1, Wb, Wb, ld, n, p, true, true, partials,
+                             counters, norm, out2, o2s, s, status));
+    return MFG_OK;
+  };
+
+  for (int64_t i = 0; i < k; ++i) {
+    // left vector: u_i = (A v_i - beta_i u_{i-1}) reorthogonalised, / alpha_i
+    MFG_LAUNCH(MFG_PROF_APPLY, ab, af,
+               apply_op<T>(A, Vb + i * ld, qb, Wb, ld, p, hiA, loA, ld, panel, status, s));
+    if (i > 0)
+      MFG_LAUNCH(MFG_PROF_SUB, 3.0 * vecb, 2.0 * vecb / sizeof(T),
+                 launch_sub<T>(U + (i - 1) * ld, qb, ld, 1, betas + i, k, 1, Wb, Wb, ld, n, p, false,
+                               true, partials, counters, norm, nullptr, 0, s, status));
+    MFG_TRY(cgs2(U, (int)i, alphas + i, k));
+    MFG_LAUNCH(MFG_PROF_SCALE, 2.0 * vecb, vecb / sizeof(T),
+               launch_scale<T>(Wb, ld, n, p, norm, U + i * ld, qb, hi, lo, ld, s));
+    // right vector: v_{i+1} = (A^T u_i - alpha_i v_i) reorthogonalised, / beta_{i+1}
+    MFG_LAUNCH(MFG_PROF_APPLY, tb, tf,
+               apply_op<T>(At, U + i * ld, qb, Wb, ld, p, hiT, loT, ld, panel, status, s));
+    MFG_LAUNCH(MFG_PROF_SUB, 3.0 * vecb, 2.0 * vecb / sizeof(T),
+               launch_sub<T>(Vb + i * ld, qb, ld, 1, alphas + i, k, 1, Wb, Wb, ld, n, p, false, true,
+                             partials, counters, norm, nullptr, 0, s, status));
+    const bool last = i + 1 == k;
+    MFG_TRY(cgs2(Vb, (int)(i + 1), last ? nullptr : betas + i + 1, k));
+    if (!last)
+      MFG_LAUNCH(MFG_PROF_SCALE, 2.0 * vecb, vecb / sizeof(T),
+                 launch_scale<T>(Wb, ld, n, p, norm, Vb + (i + 1) * ld, qb, hi, lo, ld, s));
+  }
+  // residual = beta_k v_k = the last reorthogonalised right vector (decomp.py:736)
+  if (R)
+    MFG_CUDA_TRY(cudaMemcpy2DAsync(R, ld * sizeof(T), Wb, ld * sizeof(T), ld * sizeof(T), p,
+                                   cudaMemcpyDeviceToDevice, s));
+  return MFG_OK;
+}
+
+// ---------------------------------------------------------------------------
 // Conjugate gradients (jax.scipy.sparse.linalg.cg with x0 = 0 and no
 // preconditioner, one independent solve per probe row of the panel)
 // ---------------------------------------------------------------------------
@@ -841,6 +1001,74 @@ int mfg_slq(const mfg_operator *op, int64_t k, int64_t p, const void *probes, in
              launch_tridiag_quadrature(k, p, Hb, fun, param, scale, values,
                                        reinterpret_cast<double *>(ws + L.eig),
                                        reinterpret_cast<double *>(ws + L.fsq), status, s));
+  if (mean_sem) MFG_LAUNCH(MFG_PROF_QUAD, 8.0 * p, 3.0 * p, launch_mean_sem(values, p, mean_sem, s));
+  return MFG_OK;
+}
+
+static int check_bidiag_ops(const mfg_operator *A, const mfg_operator *At, int64_t p, int64_t ld) {
+  MFG_TRY(check_op(A));
+  MFG_TRY(check_op(At));
+  if (A->n != At->n || elem_size_for(A) != elem_size_for(At)) return MFG_ERR_BAD_ARG;
+  return check_panel(A, p, ld);
+}
+
+size_t mfg_bidiag_workspace_bytes(const mfg_operator *A, const mfg_operator *At, int64_t k,
+                                  int64_t p, int64_t ld) {
+  if (check_bidiag_ops(A, At, p, ld) != MFG_OK || k < 0 || k > A->n) return 0;
+  return bidiag_layout(A, At, k, p, ld).total;
+}
+
+int mfg_bidiag(const mfg_operator *A, const mfg_operator *At, int64_t k, int64_t p, const void *V0,
+               int64_t ld, void *U, void *V, double *alphas, double *betas, void *residual,
+               double *init_len_inv, void *workspace, size_t workspace_bytes, void *stream) {
+  MFG_TRY(check_bidiag_ops(A, At, p, ld));
+  if (k < 0 || k > A->n) return MFG_ERR_RANGE;
+  if (!V0 || !aligned16(V0) || (k > 0 && (!U || !V || !alphas || !betas))) return MFG_ERR_BAD_ARG;
+  if ((U && !aligned16(U)) || (V && !aligned16(V)) || (residual && !aligned16(residual)))
+    return MFG_ERR_BAD_ARG;
+  const BidiagLayout L = bidiag_layout(A, At, k, p, ld);
+  if (!workspace || workspace_bytes < L.total) return MFG_ERR_WORKSPACE;
+  char *ws = ws_base(workspace);
+  cudaStream_t s = as_stream(stream);
+  if (A->precision == MFG_PREC_FP64)
+    return run_bidiag<double>(A, At, k, p, (const double *)V0, ld, (double *)U, (double *)V, alphas,
+                              betas, (double *)residual, init_len_inv, L, ws, s);
+  return run_bidiag<float>(A, At, k, p, (const float *)V0, ld, (float *)U, (float *)V, alphas, betas,
+                           (float *)residual, init_len_inv, L, ws, s);
+}
+
+int mfg_slq_product(const mfg_operator *A, const mfg_operator *At, int64_t k, int64_t p,
+                    const void *probes, int64_t ld, int32_t fun, double param, double *values,
+                    double *mean_sem, void *workspace, size_t workspace_bytes, void *stream) {
+  MFG_TRY(check_bidiag_ops(A, At, p, ld));
+  if (k < 1 || k > A->n) return MFG_ERR_RANGE;
+  if (!probes || !aligned16(probes) || !values) return MFG_ERR_BAD_ARG;
+  if (fun < MFG_FUN_LOG || fun > MFG_FUN_POW) return MFG_ERR_BAD_ARG;
+  const BidiagLayout L = bidiag_layout(A, At, k, p, ld);
+  if (!workspace || workspace_bytes < L.total) return MFG_ERR_WORKSPACE;
+  char *ws = ws_base(workspace);
+  cudaStream_t s = as_stream(stream);
+  double *alphas = reinterpret_cast<double *>(ws + L.alphas);
+  double *betas = reinterpret_cast<double *>(ws + L.betas);
+  double *gram = reinterpret_cast<double *>(ws + L.gram);
+  double *len0 = reinterpret_cast<double *>(ws + L.base.len0);
+  double *scale = reinterpret_cast<double *>(ws + L.values);
+  int *status = reinterpret_cast<int *>(ws + L.base.status);
+  if (A->precision == MFG_PREC_FP64)
+    MFG_TRY(run_bidiag<double>(A, At, k, p, (const double *)probes, ld, (double *)(ws + L.u),
+                               (double *)(ws + L.v), alphas, betas, nullptr, nullptr, L, ws, s));
+  else
+    MFG_TRY(run_bidiag<float>(A, At, k, p, (const float *)probes, ld, (float *)(ws + L.u),
+                              (float *)(ws + L.v), alphas, betas, nullptr, nullptr, L, ws, s));
+  // funm.py:286-303: length^2 * e1^T f(B^T B) e1 through the eigenpairs of B^T B
+  MFG_CUDA_TRY(cudaMemsetAsync(gram, 0, (size_t)p * k * k * 8, s));
+  bidiag_gram_kernel<<<(unsigned)ceil_div(p * k, 128), 128, 0, s>>>(alphas, betas, k, p, gram);
+  MFG_TRY(MFG_LAUNCH_STATUS());
+  MFG_LAUNCH(MFG_PROF_OTHER, 16.0 * p, (double)p, launch_square(len0, scale, p, s));
+  MFG_LAUNCH(MFG_PROF_QUAD, 8.0 * p * k * k + 16.0 * p * k, 0.0,
+             launch_tridiag_quadrature(k, p, gram, fun, param, scale, values,
+                                       reinterpret_cast<double *>(ws + L.base.eig),
+                                       reinterpret_cast<double *>(ws + L.base.fsq), status, s));
   if (mean_sem) MFG_LAUNCH(MFG_PROF_QUAD, 8.0 * p, 3.0 * p, launch_mean_sem(values, p, mean_sem, s));
   return MFG_OK;
 }

@@ -180,6 +180,143 @@ def tridiag_sym(num_matvecs: int, /, *, materialize: bool = True, reortho: str =
     raise ValueError(msg)
 
 
+class _Bidiag:
+    """Golub-Kahan bidiagonalisation with full reorthogonalisation (matfree/decomp.py:608-750).
+
+    The iteration runs in ``libmatfree_gb300`` (``mfg_bidiag``) for all rows
+    of a panel at once.  The vector-matrix product u -> A^T u comes from the
+    operator's ``transpose()`` (dense descriptors) or, for a callable matvec,
+    from ``torch.func.vjp`` of it, as matfree uses ``jax.vjp``
+    (decomp.py:711-725).  Rectangular maps (n_rows != n_cols) are handled by
+    zero-padding both spaces to the larger size: padded coordinates stay
+    exactly zero, so the iteration is the unpadded one.
+    """
+
+    def __init__(self, num_matvecs: int, materialize: bool):
+        self.num_matvecs = int(num_matvecs)
+        self.materialize = materialize
+
+    @staticmethod
+    def _operators(Av, x_like: torch.Tensor, params):
+        """(A, A^T) as square descriptors of size N, n_rows, n_cols."""
+        from .operators import CallbackOperator, DenseOperator, Operator
+
+        ncols = x_like.shape[-1]
+        dt = x_like.dtype if x_like.dtype in (torch.float32, torch.float64) else torch.float32
+        if isinstance(Av, DenseOperator):
+            if Av.n != ncols:
+                raise ValueError(f"operator dimension {Av.n} does not match vector length {ncols}")
+            return Av, Av.transpose(), ncols, ncols
+        if isinstance(Av, Operator):
+            raise TypeError("bidiag needs a dense operator descriptor or a callable matvec")
+
+        def av(x):
+            return ravel_pytree(Av(x, *params))[0]
+
+        nrows = av(torch.zeros(ncols, dtype=dt, device=x_like.device)).numel()
+        N = max(nrows, ncols)
+
+        def pad(X):
+            out = torch.zeros((X.shape[0], N), dtype=dt, device=X.device)
+            out[:, : X.shape[1]] = X
+            return out
+
+        def rows(fn, X):
+            try:
+                return torch.vmap(fn)(X)
+            except Exception:
+                return torch.stack([fn(x) for x in X])
+
+        def A_rows(V):
+            return pad(rows(av, V[:, :ncols]))
+
+        def At_rows(U):
+            _, vjp_fn = torch.func.vjp(av, torch.zeros(ncols, dtype=dt, device=U.device))
+            return pad(rows(lambda u: vjp_fn(u)[0], U[:, :nrows]))
+
+        A = CallbackOperator(A_rows, N, dtype=dt, batched=True)
+        At = CallbackOperator(At_rows, N, dtype=dt, batched=True)
+        return A, At, nrows, ncols
+
+    def batched(self, Av, V0: torch.Tensor, *params):
+        """Bidiagonalise from every row of V0 (p, n_cols).
+
+        Returns (U (p, k, n_rows), V (p, k, n_cols), alphas (p, k), betas (p, k),
+        residual (p, n_cols), 1/||v0|| (p,)); betas[:, 0] = 0 as in matfree.
+        """
+        require_cuda(V0, "V0")
+        p, ncols = V0.shape
+        A, At, nrows, _ = self._operators(Av, V0[0], params)
+        k = self.num_matvecs
+        if k < 0 or k > min(nrows, ncols):
+            raise ValueError(_error_num_matvecs(k, maxval=min(nrows, ncols), minval=0))
+        N = A.n
+        dt = A.basis_dtype
+        V0p = torch.zeros((p, N), dtype=dt, device=V0.device)
+        V0p[:, :ncols] = V0
+        panel, ld = as_panel(V0p, N, dt)
+        kk = max(k, 1)
+        U = torch.zeros((p, kk, ld), dtype=dt, device=V0.device)
+        V = torch.zeros((p, kk, ld), dtype=dt, device=V0.device)
+        alphas = torch.zeros((p, kk), dtype=torch.float64, device=V0.device)
+        betas = torch.zeros((p, kk), dtype=torch.float64, device=V0.device)
+        R = torch.zeros((p, ld), dtype=dt, device=V0.device)
+        c = torch.zeros((p,), dtype=torch.float64, device=V0.device)
+        sA, sT = A.c_struct(), At.c_struct()
+        lib = _lib.lib()
+        nbytes = lib.mfg_bidiag_workspace_bytes(ctypes.byref(sA), ctypes.byref(sT), k, p, ld)
+        if nbytes == 0:
+            raise ValueError("unsupported operator pair for bidiagonalisation")
+        ws, wsb = _WS.get(nbytes, V0.device)
+        st = lib.mfg_bidiag(ctypes.byref(sA), ctypes.byref(sT), k, p, ctypes.c_void_p(panel.data_ptr()), ld,
+                            ctypes.c_void_p(U.data_ptr()), ctypes.c_void_p(V.data_ptr()),
+                            ctypes.c_void_p(alphas.data_ptr()), ctypes.c_void_p(betas.data_ptr()),
+                            ctypes.c_void_p(R.data_ptr()), ctypes.c_void_p(c.data_ptr()), ws, wsb, stream_ptr())
+        for op in (A, At):
+            err = getattr(op, "error", None)
+            if err is not None:
+                op.error = None
+                raise err
+        _lib.check(st, "mfg_bidiag")
+        return (U[:, :k, :nrows], V[:, :k, :ncols], alphas[:, :k], betas[:, :k], R[:, :ncols], c)
+
+    def __call__(self, Av, v0, *params) -> _DecompResult:
+        from .operators import Operator
+
+        flat, unravel = ravel_pytree(v0)
+        require_cuda(flat, "v0")
+        if isinstance(Av, Operator):
+            U, V, alphas, betas, R, c = self.batched(Av, flat[None, :], *params)
+            out_like, u_unravel = flat, unravel
+        else:
+            def av_flat(x, *p):
+                return Av(unravel(x), *p)
+
+            U, V, alphas, betas, R, c = self.batched(av_flat, flat[None, :], *params)
+            out_like = av_flat(flat, *params)
+            _, u_unravel = ravel_pytree(out_like)
+        out_dt = flat.dtype if flat.dtype in (torch.float32, torch.float64) else torch.float32
+        d, e = alphas[0].to(out_dt), betas[0, 1:].to(out_dt)
+        J = torch.diag_embed(d) + torch.diag_embed(e, 1) if self.materialize else (d, e)
+        U0, V0 = U[0].to(out_dt), V[0].to(out_dt)
+        return _DecompResult(Q_tall=(_stack_unravel(u_unravel, U0, out_like), _stack_unravel(unravel, V0, v0)),
+                             J_small=J, residual=unravel(R[0].to(out_dt)), init_length_inv=c[0].to(out_dt))
+
+
+def _stack_unravel(unravel, M: torch.Tensor, like):
+    """k stacked flat vectors (k, n) -> a stack in the shape of ``like``."""
+    if isinstance(like, torch.Tensor):
+        return M.reshape(M.shape[0], *like.shape)
+    return torch.vmap(unravel)(M)
+
+
+def bidiag(num_matvecs: int, /, materialize: bool = True, reortho: str = "full"):
+    """Golub-Kahan bidiagonalisation (matfree/decomp.py:641-750)."""
+    if reortho != "full":
+        raise NotImplementedError("bidiag is provided with full reorthogonalisation only")
+    return _Bidiag(num_matvecs, materialize)
+
+
 def hessenberg(num_matvecs, /, *, reortho: str, custom_vjp: bool = True, reortho_vjp: str = "match"):
     """Arnoldi / Hessenberg factorisation (matfree/decomp.py:353-423)."""
     reortho_expected = ["none", "full"]

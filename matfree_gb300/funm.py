@@ -187,3 +187,119 @@ def funm_lanczos_sym(dense_funm, tridiag_sym, /):
         return unravel(length * (Q.double().T @ fT[:, 0]).to(flat.dtype))
 
     return estimate
+
+
+# ---------------------------------------------------------------------------
+# Matrix functions of products A^T A (matfree/funm.py:246-320)
+# ---------------------------------------------------------------------------
+
+
+class DenseFunmProductSvd(DenseFunmSymEigh):
+    """f(B^T B) through the SVD of B (matfree/funm.py:306-320).
+
+    ``kind``/``param`` name the fused device quadrature of f on the
+    eigenvalues of B^T B (log, or x ** param for Schatten norms).
+    """
+
+    def __call__(self, matrix: torch.Tensor) -> torch.Tensor:
+        require_cuda(matrix, "matrix")
+        _, S, Vt = torch.linalg.svd(matrix)
+        eigvecs = Vt.transpose(-1, -2)
+        return eigvecs @ torch.diag_embed(self.apply_scalar(S * S)) @ eigvecs.transpose(-1, -2)
+
+
+def dense_funm_product_svd(matfun):
+    """matfree/funm.py:306-320."""
+    return DenseFunmProductSvd(matfun)
+
+
+class MonteCarloFunmProduct:
+    """The integrand ||v||^2 e1^T f(B^T B) e1 of matfree/funm.py:276-303."""
+
+    def __init__(self, dense_funm, bidiag):
+        from .decomp import _Bidiag
+
+        if not isinstance(dense_funm, DenseFunmProductSvd):
+            dense_funm = DenseFunmProductSvd(dense_funm)
+        if not isinstance(bidiag, _Bidiag):
+            raise TypeError("bidiag must come from matfree_gb300.decomp.bidiag(k)")
+        self.dense_funm = dense_funm
+        self.bidiag = bidiag
+
+    def __call__(self, matvec, v0, *parameters):
+        flat, unravel = ravel_pytree(v0)
+        require_cuda(flat, "v0")
+        if isinstance(matvec, Operator):
+            return self.batched(matvec, flat[None, :], *parameters)[0]
+
+        def flat_matvec(x, *p):
+            return ravel_pytree(matvec(unravel(x), *p))[0]
+
+        return self.batched(flat_matvec, flat[None, :], *parameters)[0]
+
+    def batched(self, matvec, samples: torch.Tensor, *parameters) -> torch.Tensor:
+        """Integrand values (p,) float64 for the rows of samples (p, n_cols)."""
+        require_cuda(samples, "samples")
+        k = self.bidiag.num_matvecs
+        if self.dense_funm.kind is not None:
+            return _slq_product_values(self.bidiag, matvec, samples, k, self.dense_funm.kind,
+                                       self.dense_funm.param, parameters)
+        _, _, alphas, betas, _, c = self.bidiag.batched(matvec, samples, *parameters)
+        lam, fsq = tridiag_eigh_first(_gram(alphas, betas))
+        return (1.0 / (c * c)) * (self.dense_funm.apply_scalar(lam) * fsq).sum(-1)
+
+
+def _gram(alphas: torch.Tensor, betas: torch.Tensor) -> torch.Tensor:
+    """B^T B (p, k, k) for the upper bidiagonal B (alphas; betas[:, 1:] above)."""
+    p, k = alphas.shape
+    d = alphas * alphas
+    d[:, 1:] += betas[:, 1:] * betas[:, 1:]
+    o = alphas[:, :-1] * betas[:, 1:]
+    return torch.diag_embed(d) + torch.diag_embed(o, 1) + torch.diag_embed(o, -1)
+
+
+def _slq_product_values(bidiag, matvec, samples, k, kind, param, parameters):
+    """One ``mfg_slq_product`` call for all rows of samples."""
+    p, ncols = samples.shape
+    A, At, nrows, _ = bidiag._operators(matvec, samples[0], parameters)
+    if k < 1 or k > min(nrows, ncols):
+        from .decomp import _error_num_matvecs
+
+        raise ValueError(_error_num_matvecs(k, maxval=min(nrows, ncols), minval=0))
+    N = A.n
+    dt = A.basis_dtype
+    V0p = torch.zeros((p, N), dtype=dt, device=samples.device)
+    V0p[:, :ncols] = samples
+    panel, ld = as_panel(V0p, N, dt)
+    values = torch.empty((p,), dtype=torch.float64, device=samples.device)
+    sA, sT = A.c_struct(), At.c_struct()
+    lib = _lib.lib()
+    nbytes = lib.mfg_bidiag_workspace_bytes(ctypes.byref(sA), ctypes.byref(sT), k, p, ld)
+    if nbytes == 0:
+        raise ValueError("unsupported operator pair for bidiagonalisation")
+    ws, wsb = _WS.get(nbytes, samples.device)
+    st = lib.mfg_slq_product(ctypes.byref(sA), ctypes.byref(sT), k, p, ctypes.c_void_p(panel.data_ptr()), ld,
+                             kind, param, ctypes.c_void_p(values.data_ptr()), None, ws, wsb, stream_ptr())
+    for op in (A, At):
+        err = getattr(op, "error", None)
+        if err is not None:
+            op.error = None
+            raise err
+    _lib.check(st, "mfg_slq_product")
+    return values
+
+
+def monte_carlo_funm_product(dense_funm, bidiag, /):
+    """matfree/funm.py:276-303."""
+    return MonteCarloFunmProduct(dense_funm, bidiag)
+
+
+def monte_carlo_funm_product_logdet(bidiag, /):
+    """matfree/funm.py:246-256: log det(A^T A)."""
+    return MonteCarloFunmProduct(DenseFunmProductSvd(torch.log, kind=_lib.MFG_FUN_LOG), bidiag)
+
+
+def monte_carlo_funm_product_schatten_norm(power, bidiag, /):
+    """matfree/funm.py:259-273: the power-th power of the Schatten-power norm."""
+    fn = DenseFunmProductSvd(lambda x: x ** (power / 2), kind=_lib.MFG_FUN_POW, param=power / 2)
+    return MonteCarloFunmProduct(fn, bidiag)

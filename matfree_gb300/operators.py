@@ -123,6 +123,25 @@ class DenseOperator(Operator):
         s.shift = self.shift
         return s
 
+    def transpose(self) -> "DenseOperator":
+        """A^T + shift I in the same storage (an explicit transposed copy, cached)."""
+        cached = getattr(self, "_transpose", None)
+        if cached is not None:
+            return cached
+        n = self.n
+
+        def tr(a):
+            if a is None:
+                return None
+            t = torch.zeros_like(a)
+            t[:, :n] = a[:, :n].t()
+            return t
+
+        out = DenseOperator._from_storage(n, self.precision, tr(self.a), tr(self.a_lo), self.shift)
+        out._transpose = self
+        self._transpose = out
+        return out
+
     def dense(self) -> torch.Tensor:
         """The operator as a float64 (n, n) matrix (for checks)."""
         a = self.a[:, : self.n].double()

@@ -60,6 +60,7 @@ class _Samples:
 
     def __init__(self, flat, unravel):
         self.flat = flat
+        self.unravel = unravel  # one flat row -> one pytree sample
         self.tree = unravel(flat)
 
 
@@ -81,7 +82,7 @@ def _evaluate(integrand, matvec, samples, parameters):
     if hasattr(integrand, "batched") and isinstance(flat, torch.Tensor) and flat.dim() == 2:
         if isinstance(samples, _Samples) and not hasattr(matvec, "c_struct"):
             # pytree probes with a pytree matvec: flatten the matvec
-            unravel = ravel_pytree(samples.tree)[1]
+            unravel = samples.unravel
 
             def flat_matvec(v, *p):
                 return ravel_pytree(matvec(_unbatch(unravel, v), *p))[0]

@@ -59,3 +59,11 @@ def laplacian_2d(m, shift=0.1):
     A.sort_indices()
     A = sp.csr_matrix((A.data.astype(np.float32), A.indices.astype(np.int32), A.indptr.astype(np.int32)), shape=(n, n))
     return A
+
+
+def asymmetric_matrix_from_singular_values(vals, nrows, ncols):
+    """matfree/test_util.py:33-38: a fixed (nrows, ncols) matrix with singular values vals."""
+    A = np.reshape(np.arange(1.0, nrows * ncols + 1.0), (nrows, ncols))
+    A /= nrows * ncols
+    U, _S, Vt = np.linalg.svd(A, full_matrices=False)
+    return U @ np.diag(np.asarray(vals, dtype=np.float64)) @ Vt
