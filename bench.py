@@ -570,8 +570,9 @@ def product_arm(args):
     torch.cuda.set_device(0)
     n, k, p = 8192, 32, 128
     rng = np.random.default_rng(0)
-    # singular values in about [0.5, 1.5]: well conditioned for an fp32 basis
-    A = (0.5 * rng.standard_normal((n, n)) / math.sqrt(n) + np.eye(n)).astype(np.float32)
+    # singular values in about [1.5, 2.5]: well conditioned, and log det(A^T A)
+    # far from zero, so that relative errors are meaningful
+    A = (0.5 * rng.standard_normal((n, n)) / math.sqrt(n) + 2.0 * np.eye(n)).astype(np.float32)
     op = mf.DenseOperator(torch.from_numpy(A).cuda(), precision=args.precision)
     op.transpose()  # the transposed copy is built once, outside the timed steps
     key = mf.prng.prng_key(1)
@@ -601,7 +602,7 @@ def product_arm(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": f"f32 basis / {args.precision} operator / f64 reductions",
             "data": "synthetic (seeded)",
-            "config": {"workload": f"log det(A^T A), A = I + 0.5 N(0,1)/sqrt(n), n={n}, k={k}, p={p} Rademacher probes, "
+            "config": {"workload": f"log det(A^T A), A = 2 I + 0.5 N(0,1)/sqrt(n), n={n}, k={k}, p={p} Rademacher probes, "
                                    f"operator {args.precision}"},
             "estimate": float(val),
             "rel_err_vs_fp64_oracle": {"value": abs(gpu_first - ref) / abs(ref), "on": f"first {num} probes"},
@@ -650,7 +651,7 @@ def serve_arm(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=12)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="rbf16k", choices=sorted(CONFIGS) + ["serve", "grad8k", "gp8k", "product8k"])

@@ -234,8 +234,9 @@ MFG_API size_t mfg_cg_workspace_bytes(const mfg_operator *op, int64_t p, int64_t
  * max(tol^2 ||b||^2, atol^2) or after maxiter iterations (maxiter <= 0:
  * 10 n), and stays unchanged while the other rows iterate.  iters (device,
  * p int32, may be NULL) receives the iterations each row ran.  Synchronises
- * `stream` once per iteration (to test whether any row still runs); returns
- * the first device-side error status (e.g. MFG_ERR_TIMEOUT) or MFG_OK. */
+ * `stream` every 8 iterations to test whether any row still runs (finished
+ * rows stay unchanged meanwhile); returns the first device-side error status
+ * (e.g. MFG_ERR_TIMEOUT) or MFG_OK. */
 MFG_API int mfg_cg(const mfg_operator *op, int64_t p, const void *B, void *X, int64_t ld,
                    double tol, double atol, int64_t maxiter, int32_t *iters, void *workspace,
                    size_t workspace_bytes, void *stream);

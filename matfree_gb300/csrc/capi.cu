@@ -646,6 +646,8 @@ static int run_bidiag(const mfg_operator *A, const mfg_operator *At, int64_t k, 
 // preconditioner, one independent solve per probe row of the panel)
 // ---------------------------------------------------------------------------
 
+constexpr int64_t kCgCheckEvery = 8;  // iterations between host convergence tests
+
 struct CgLayout {
   size_t r, p, w, hi, lo, rs0, rs1, pap, thr, partials, counters, nactive, status, iters, total;
 };
@@ -718,6 +720,9 @@ static int run_cg(const mfg_operator *op, int64_t p, const T *B, T *X, int64_t l
                                    nactive, iters, s));
     MFG_LAUNCH(MFG_PROF_SCALE, 3.0 * vecb, 2.0 * vecb / sizeof(T),
                launch_cg_direction<T>(P, R, ld, n, p, rc, rn, thr, hi, lo, s));
+    // test for convergence every kCgCheckEvery iterations (and at the end):
+    // a finished row only runs frozen (alpha = 0) iterations until then
+    if ((it + 1) % kCgCheckEvery != 0 && it + 1 < maxiter) continue;
     int host_active = 0;
     MFG_CUDA_TRY(cudaMemcpyAsync(&host_active, nactive, sizeof(int), cudaMemcpyDeviceToHost, s));
     MFG_CUDA_TRY(cudaStreamSynchronize(s));
