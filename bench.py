@@ -310,9 +310,26 @@ def gpu_arm(args):
         e2e = {"value": world * args.steps / e2e_s, "unit": UNIT,
                "h2d_bytes_per_step": int(x_host.numel() * 4), "d2h_bytes_per_step": 16}
 
+    # (4) the plain per-request FP32 drop-in on the same problem: fp32 operator
+    # on the CUDA cores, one solve at a time (the comparison the metric names)
+    plain = None
+    if kind == "rbf" and precision != "fp32" and rank == 0 and not args.no_plain_fp32:
+        def plain_solve():
+            op = mf.RBFKernelOperator(x_dev, s2=prob["s2"], ell=prob["ell"], tau=prob["tau"],
+                                      precision="fp32")
+            return slq_values(op, k, sampler(key), _lib.MFG_FUN_LOG, 0.0, workspace=slots[0].ws)
+
+        plain_solve()
+        torch.cuda.synchronize()
+        t_p = time.perf_counter()
+        for _ in range(2):
+            pv = plain_solve()
+        torch.cuda.synchronize()
+        plain = {"solves_per_s": 2.0 / (time.perf_counter() - t_p), "values": pv}
+
     result = {"rank": rank, "world": world, "total_ms": total_ms, "step_ms": step_ms, "prof": prof,
               "clocks": clocks, "estimate": est, "e2e": e2e, "values": values, "key": key,
-              "launches": launches}
+              "launches": launches, "plain": plain}
     return result, prob
 
 
@@ -665,6 +682,8 @@ def main():
     ap.add_argument("--precision", default="bf16x3", choices=["fp32", "bf16", "bf16x3", "fp64"])
     ap.add_argument("--cpu-probes", type=int, default=8)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain-fp32", action="store_true",
+                    help="skip the plain per-request fp32 comparison solves")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -720,6 +739,15 @@ def main():
             "sample": f"{num} of {prob['p']} probes at full n and k (float64 NumPy restatement, "
                       f"{secs:.1f} s incl. {build:.1f} s operator build); extrapolated linearly in probes"}
         line["rel_err_vs_fp64"] = {"value": rel, "on": f"mean over the first {num} probes, identical probe vectors"}
+    if res["plain"] is not None:
+        pl = res["plain"]
+        line["plain_fp32_per_request"] = {
+            "solves_per_s": pl["solves_per_s"], "speedup": value / pl["solves_per_s"],
+            "note": "same problem, fp32 operator on the CUDA cores, one solve at a time"}
+        if not args.no_cpu_baseline:
+            pvals = pl["values"][:num].cpu().numpy()
+            line["plain_fp32_per_request"]["rel_err_vs_fp64"] = float(
+                abs(pvals.mean() - vals.mean()) / abs(vals.mean()))
     print(json.dumps(line), flush=True)
 
 

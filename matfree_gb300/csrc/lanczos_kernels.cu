@@ -401,10 +401,21 @@ scale_kernel(const T *__restrict__ Win, int64_t w_bstride, int64_t n, const doub
       h[u] = __float2bfloat16_rn(x);
       l[u] = __float2bfloat16_rn(x - __bfloat162float(h[u]));
     }
+    if constexpr (W == 4) {
+      // four bf16 per 8-byte store (r is a multiple of 4, the rows 16-byte aligned)
+      uint2 hv, lv;
+      hv.x = (uint32_t)__bfloat16_as_ushort(h[0]) | ((uint32_t)__bfloat16_as_ushort(h[1]) << 16);
+      hv.y = (uint32_t)__bfloat16_as_ushort(h[2]) | ((uint32_t)__bfloat16_as_ushort(h[3]) << 16);
+      lv.x = (uint32_t)__bfloat16_as_ushort(l[0]) | ((uint32_t)__bfloat16_as_ushort(l[1]) << 16);
+      lv.y = (uint32_t)__bfloat16_as_ushort(l[2]) | ((uint32_t)__bfloat16_as_ushort(l[3]) << 16);
+      *reinterpret_cast<uint2 *>(hi + b * bf_bstride + r) = hv;
+      if (lo) *reinterpret_cast<uint2 *>(lo + b * bf_bstride + r) = lv;
+    } else {
 #pragma unroll
-    for (int u = 0; u < W; ++u) {
-      hi[b * bf_bstride + r + u] = h[u];
-      if (lo) lo[b * bf_bstride + r + u] = l[u];
+      for (int u = 0; u < W; ++u) {
+        hi[b * bf_bstride + r + u] = h[u];
+        if (lo) lo[b * bf_bstride + r + u] = l[u];
+      }
     }
   }
 }
