@@ -183,6 +183,7 @@ class _Slot:
         self.mean_sem = torch.zeros(2, dtype=torch.float64, device=dev)
         self.host = torch.zeros(2, dtype=torch.float64).pin_memory()
         self.done = torch.cuda.Event()
+        self.pending = None  # inputs of the solve in flight, until its status is read
 
 
 def gpu_arm(args):
@@ -192,7 +193,7 @@ def gpu_arm(args):
 
     import matfree_gb300 as mf
     from matfree_gb300 import _lib
-    from matfree_gb300.funm import slq_values
+    from matfree_gb300.funm import slq_retry_needed, slq_values
 
     rank, world, local = _dist_init(args.gpus)
     prob = build_problem(args.config)
@@ -214,8 +215,11 @@ def gpu_arm(args):
     sampler = mf.stochtrace.sampler_signs(torch.ones(n, device=dev), num=p)
     slots = [_Slot(torch, dev) for _ in range(max(1, args.inflight))]
 
-    def solve(x, slot, h2d=False):
-        """One complete solve enqueued on the slot's stream."""
+    retries = [0]
+
+    def solve(x, slot, h2d=False, two_sweep=None):
+        """One complete solve enqueued on the slot's stream (its device status is
+        read by finish() once the slot is reused)."""
         with torch.cuda.stream(slot.stream):
             if h2d:
                 x = x_host.to(dev, non_blocking=True)
@@ -226,11 +230,26 @@ def gpu_arm(args):
                 op = static
             V = sampler(key)
             vals = slq_values(op, k, V, _lib.MFG_FUN_LOG, 0.0, mean_sem=slot.mean_sem,
-                              workspace=slot.ws)
+                              workspace=slot.ws, two_sweep=two_sweep, check=False)
             if h2d:
                 slot.host.copy_(slot.mean_sem, non_blocking=True)
             slot.done.record(slot.stream)
+            slot.pending = (x, h2d)
         return vals
+
+    def finish(slot):
+        """Wait for the slot's solve; repeat it with the three-sweep form if the
+        two-sweep step reported MFG_ERR_RETRY."""
+        if slot.pending is None:
+            return
+        x, h2d = slot.pending
+        slot.pending = None
+        with torch.cuda.stream(slot.stream):
+            if slq_retry_needed(slot.ws):
+                retries[0] += 1
+                solve(x, slot, h2d, two_sweep=False)
+                slot.pending = None
+                slot.done.synchronize()
 
     def join_all():
         cur = torch.cuda.current_stream()
@@ -242,7 +261,10 @@ def gpu_arm(args):
             s.stream.wait_stream(torch.cuda.current_stream())
 
     for i in range(args.warmup):
+        finish(slots[i % len(slots)])
         solve(x_dev, slots[i % len(slots)])
+    for s_ in slots:
+        finish(s_)
     join_all()
     torch.cuda.synchronize()
     lib = _lib.lib()
@@ -260,9 +282,12 @@ def gpu_arm(args):
         fork_all()
         for i in range(args.steps):
             slot = slots[i % len(slots)]
+            finish(slot)  # the solve this slot ran before: done, status read
             starts[i].record(slot.stream)
             values = solve(x_dev, slot)
             ends[i].record(slot.stream)
+        for s_ in slots:
+            finish(s_)
         join_all()
         t1.record()
         torch.cuda.synchronize()
@@ -280,7 +305,9 @@ def gpu_arm(args):
     lib.mfg_profile_enable(1)
     torch.cuda.synchronize()
     for i in range(args.steps):
+        finish(slots[0])
         solve(x_dev, slots[0])
+    finish(slots[0])
     torch.cuda.synchronize()
     ms = (ctypes.c_double * nc)()
     by = (ctypes.c_double * nc)()
@@ -301,10 +328,12 @@ def gpu_arm(args):
             slot = slots[i % len(slots)]
             if i >= len(slots):
                 slot.done.synchronize()
+                finish(slot)
                 _ = float(slot.host[0])  # the result of the solve this slot ran before
             solve(None, slot, h2d=True)
         for i in range(max(0, args.steps - len(slots)), args.steps):
             slots[i % len(slots)].done.synchronize()
+            finish(slots[i % len(slots)])
             _ = float(slots[i % len(slots)].host[0])
         e2e_s = _max_over_ranks(time.perf_counter() - t_start, world)
         e2e = {"value": world * args.steps / e2e_s, "unit": UNIT,
@@ -329,7 +358,7 @@ def gpu_arm(args):
 
     result = {"rank": rank, "world": world, "total_ms": total_ms, "step_ms": step_ms, "prof": prof,
               "clocks": clocks, "estimate": est, "e2e": e2e, "values": values, "key": key,
-              "launches": launches, "plain": plain}
+              "launches": launches, "plain": plain, "two_sweep_retries": retries[0]}
     return result, prob
 
 
@@ -337,6 +366,11 @@ def gpu_arm(args):
 # capture of that exact launch: --set full on `--config rbf16k4` (the same operator and
 # panel as rbf16k), kernel dense_tcgen05_pair_kernel<1>: 1.107433 GB read + 3.28 MB written.
 TRAFFIC = {("rbf16k", "bf16x3", "operator apply"): 1.107433e9 + 3.27936e6}
+
+
+def _two_sweep(args, prob):
+    """Whether the solves ran the two-sweep step (float bases, 2 <= k <= 65)."""
+    return args.precision != "fp64" and 2 <= prob["k"] <= 65
 
 
 def roofline(prof, peaks, steps, config=None, precision=None):
@@ -726,6 +760,9 @@ def main():
         "estimate": res["estimate"], "roofline": rl, "gpu_launches": launches,
         "clocks": res["clocks"], "e2e": res["e2e"],
         "kernel_ms_per_step": {c: v["ms"] / args.steps for c, v in res["prof"].items()},
+        "reortho": {"form": "two reads of the basis per step" if _two_sweep(args, prob)
+                    else "three reads of the basis per step",
+                    "retries": res["two_sweep_retries"]},
     }
     if not args.no_cpu_baseline:
         num = args.cpu_probes

@@ -43,7 +43,9 @@ enum {
   MFG_ERR_UNSUPPORTED = 5, /* combination not implemented (e.g. op/precision) */
   MFG_ERR_NO_CONVERGENCE = 6, /* tridiagonal eigensolver hit its sweep limit  */
   MFG_ERR_TIMEOUT = 7,     /* a bounded device-side wait gave up             */
-  MFG_ERR_SCRATCH_LIMIT = 8 /* problem larger than a fixed static scratch     */
+  MFG_ERR_SCRATCH_LIMIT = 8, /* problem larger than a fixed static scratch    */
+  MFG_ERR_RETRY = 9         /* two-sweep reorthogonalisation lost accuracy:   */
+                            /* repeat the call with reortho = 1               */
 };
 
 /* ---- element type of vectors and bases --------------------------------- */
@@ -129,7 +131,11 @@ MFG_API int mfg_operator_apply(const mfg_operator *op, const void *V, void *W, i
  * (matfree/decomp.py:30-152, 353-477).  reortho: 1 = "full" (Gram-Schmidt
  * twice against all vectors), 0 = "none" of hessenberg (once against all
  * vectors), 2 = three-term Lanczos of tridiag_sym(reortho="none")
- * (decomp.py:215-291: H holds a_j on the diagonal and b_j below it). */
+ * (decomp.py:215-291: H holds a_j on the diagonal and b_j below it),
+ * 3 = "full" in two basis reads per step (see MFG_SLQ_TWO_SWEEP; falls back
+ * to 1 outside float bases with 2 <= k <= 65; workspace from
+ * mfg_slq_ex_workspace_bytes(..., MFG_SLQ_TWO_SWEEP); check
+ * mfg_workspace_status for MFG_ERR_RETRY). */
 MFG_API int mfg_hessenberg(const mfg_operator *op, int64_t k, int64_t p, const void *V,
                    int64_t ld, int32_t reortho, void *Q, double *H, void *residual,
                    double *init_len_inv, void *workspace, size_t workspace_bytes,
@@ -176,6 +182,32 @@ MFG_API int mfg_tridiag_quadrature(int64_t k, int64_t p, const double *H, int32_
 MFG_API int mfg_slq(const mfg_operator *op, int64_t k, int64_t p, const void *probes,
             int64_t ld, int32_t fun, double param, double *values, double *mean_sem,
             void *Q, double *H, void *workspace, size_t workspace_bytes, void *stream);
+
+/* mfg_slq with options.  MFG_SLQ_TWO_SWEEP: the same full reorthogonalisation
+ * in two reads of the Krylov basis per step instead of three (the second
+ * projection of step j-1 is done together with the first projection of step
+ * j, and A q_j is recovered from A applied to the not yet reorthogonalised
+ * vector through the Arnoldi relation).  H, and so values, equal mfg_slq's to
+ * rounding.  Applies to float bases with 2 <= k <= 65 (otherwise the call
+ * runs mfg_slq).  When a step's second projection exceeds 0.1 of the vector
+ * (a vector left largely inside the basis by one projection, near an
+ * invariant subspace) the rounding of the recovered product is no longer
+ * negligible: the run then records MFG_ERR_RETRY in the workspace, read back
+ * with mfg_workspace_status, and the caller repeats the call without the
+ * flag.  Workspace: mfg_slq_ex_workspace_bytes with the same flags. */
+enum { MFG_SLQ_TWO_SWEEP = 1 };
+MFG_API size_t mfg_slq_ex_workspace_bytes(const mfg_operator *op, int64_t k, int64_t p, int64_t ld,
+                                          int32_t flags);
+MFG_API int mfg_slq_ex(const mfg_operator *op, int64_t k, int64_t p, const void *probes,
+                       int64_t ld, int32_t fun, double param, double *values, double *mean_sem,
+                       void *Q, double *H, int32_t flags, void *workspace,
+                       size_t workspace_bytes, void *stream);
+
+/* Waits for `stream` and returns the device-side status of the last
+ * mfg_slq / mfg_slq_ex / mfg_hessenberg run on this workspace: MFG_OK,
+ * MFG_ERR_RETRY, MFG_ERR_NO_CONVERGENCE or MFG_ERR_TIMEOUT (the host return
+ * code of the call reports launch-time errors only). */
+MFG_API int mfg_workspace_status(const void *workspace, void *stream);
 
 /* Dense RBF kernel matrix K_ij = s2 exp(-|x_i - x_j|^2 / (2 ell^2)) from
  * points x (n x dim float32, row-major), WITHOUT the nugget (pass tau as the

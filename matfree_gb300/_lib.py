@@ -21,6 +21,8 @@ MFG_ERR_UNSUPPORTED = 5
 MFG_ERR_NO_CONVERGENCE = 6
 MFG_ERR_TIMEOUT = 7
 MFG_ERR_SCRATCH_LIMIT = 8
+MFG_ERR_RETRY = 9
+MFG_SLQ_TWO_SWEEP = 1
 
 MFG_F32, MFG_F64 = 0, 1
 MFG_OP_DENSE, MFG_OP_CSR, MFG_OP_CALLBACK = 0, 1, 2
@@ -62,6 +64,9 @@ SIGNATURES = {
     "mfg_hessenberg": (c_int, [POINTER(MfgOperator), c_int64, c_int64, c_void_p, c_int64, c_int32, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
     "mfg_tridiag_quadrature": (c_int, [c_int64, c_int64, c_void_p, c_int32, c_double, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     "mfg_slq": (c_int, [POINTER(MfgOperator), c_int64, c_int64, c_void_p, c_int64, c_int32, c_double, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
+    "mfg_slq_ex_workspace_bytes": (c_size_t, [POINTER(MfgOperator), c_int64, c_int64, c_int64, c_int32]),
+    "mfg_slq_ex": (c_int, [POINTER(MfgOperator), c_int64, c_int64, c_void_p, c_int64, c_int32, c_double, c_void_p, c_void_p, c_void_p, c_void_p, c_int32, c_void_p, c_size_t, c_void_p]),
+    "mfg_workspace_status": (c_int, [c_void_p, c_void_p]),
     "mfg_rbf_build": (c_int, [c_void_p, c_int64, c_int32, c_double, c_double, c_int32, c_void_p, c_void_p, c_int64, c_void_p]),
     "mfg_rbf_build_dlogell": (c_int, [c_void_p, c_int64, c_int32, c_double, c_double, c_int32, c_void_p, c_void_p, c_int64, c_void_p]),
     "mfg_split_bf16": (c_int, [c_void_p, c_int64, c_int64, c_int64, c_void_p, c_void_p, c_int64, c_void_p]),

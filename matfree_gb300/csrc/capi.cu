@@ -87,11 +87,21 @@ static void prof_end(size_t e0, int cls, double bytes, double flops, cudaStream_
   } while (0)
 
 struct WsLayout {
-  size_t w, panel, norm, len0, h2, partials, counters, status, hi, lo, q, h, values, eig, fsq, total;
+  size_t w, panel, norm, len0, h2, partials, counters, status, hi, lo, q, h, values, eig, fsq;
+  // two-sweep Arnoldi: qt (float panel), X2 (p (2k + 1)), dots (p 3), nu (p),
+  // finish coefficients (p 4), full coefficients Hh (p (k + 1) k)
+  size_t vt, x2, dots, nu, cf, hh;
+  size_t total;
 };
 
 static int elem_size_for(const mfg_operator *op) {
   return op->precision == MFG_PREC_FP64 ? 8 : 4;
+}
+
+// The two-sweep step covers float bases of up to 65 vectors (its two-vector
+// passes keep both vectors' per-thread sums in registers).
+static bool two_sweep_applies(const mfg_operator *op, int64_t k) {
+  return op->precision != MFG_PREC_FP64 && k >= 2 && k <= kTwoSweepMaxCols + 1;
 }
 
 static bool uses_bf16(const mfg_operator *op) {
@@ -99,7 +109,9 @@ static bool uses_bf16(const mfg_operator *op) {
          (op->precision == MFG_PREC_BF16 || op->precision == MFG_PREC_BF16X3);
 }
 
-static WsLayout layout(const mfg_operator *op, int64_t k, int64_t p, int64_t ld) {
+// The device status word comes first, so that mfg_workspace_status can find
+// it without the problem sizes.
+static WsLayout layout(const mfg_operator *op, int64_t k, int64_t p, int64_t ld, bool two = false) {
   WsLayout L{};
   const size_t es = (size_t)elem_size_for(op);
   // the fused update+projection uses the smallest chunks (256 rows)
@@ -111,14 +123,16 @@ static WsLayout layout(const mfg_operator *op, int64_t k, int64_t p, int64_t ld)
     off = align_up(off + bytes, 256);
     return o;
   };
+  L.status = take(16);
   L.w = take((size_t)p * ld * es);
   L.panel = take(op->kind == MFG_OP_CALLBACK ? (size_t)p * ld * es : 0);
   L.norm = take((size_t)p * 8);
   L.len0 = take((size_t)p * 8);
   L.h2 = take((size_t)p * kk * 8);
-  L.partials = take((size_t)p * nch * (kk + 1) * 8);
+  // partial sums per probe and CTA: k + 1 values, 2 (8 ceil(k / 8)) + 1 for
+  // the two-vector projections
+  L.partials = take((size_t)p * nch * (two ? 2 * kk + 64 : kk + 1) * 8);
   L.counters = take((size_t)p * 4);
-  L.status = take(16);
   L.hi = take(uses_bf16(op) ? (size_t)p * ld * 2 : 0);
   L.lo = take(uses_bf16(op) && op->precision == MFG_PREC_BF16X3 ? (size_t)p * ld * 2 : 0);
   L.q = take((size_t)p * kk * ld * es);
@@ -126,6 +140,14 @@ static WsLayout layout(const mfg_operator *op, int64_t k, int64_t p, int64_t ld)
   L.values = take((size_t)p * 8);
   L.eig = take((size_t)p * kk * 8);
   L.fsq = take((size_t)p * kk * 8);
+  if (two) {
+    L.vt = take((size_t)p * ld * es);
+    L.x2 = take((size_t)p * (2 * kk + 1) * 8);
+    L.dots = take((size_t)p * 3 * 8);
+    L.nu = take((size_t)p * 8);
+    L.cf = take((size_t)p * 4 * 8);
+    L.hh = take((size_t)p * (kk + 1) * kk * 8);
+  }
   L.total = off + 256;  // slack for aligning the caller's base pointer
   return L;
 }
@@ -224,6 +246,86 @@ static void apply_cost(const mfg_operator *op, int64_t p, double *bytes, double 
   }
 }
 
+// Full reorthogonalisation in two reads of the basis per step (the second
+// projection of step j - 1 is done with the first of step j; see the
+// two-sweep notes in lanczos_kernels.cu).  Q row 0 and its bf16 copies are
+// in place.  H holds what the reference's H holds; R (optional) is the
+// reference's residual w''_{k-1}.  A step whose second projection is large
+// raises MFG_ERR_RETRY in the device status word.
+template <typename T>
+static int run_two_sweep(const mfg_operator *op, int64_t k, int64_t p, int64_t ld, T *Q,
+                         double *H, T *R, const WsLayout &L, char *ws, cudaStream_t s) {
+  if constexpr (sizeof(T) != 4) {
+    return MFG_ERR_UNSUPPORTED;
+  } else {
+    const int64_t n = op->n;
+    const double vecb = (double)n * (double)p * (double)sizeof(T);
+    double ab = 0.0, af = 0.0;
+    apply_cost(op, p, &ab, &af);
+    T *Wb = reinterpret_cast<T *>(ws + L.w);
+    T *panel = reinterpret_cast<T *>(ws + L.panel);
+    T *Vt = reinterpret_cast<T *>(ws + L.vt);
+    double *X2 = reinterpret_cast<double *>(ws + L.x2);
+    double *dots = reinterpret_cast<double *>(ws + L.dots);
+    double *nu = reinterpret_cast<double *>(ws + L.nu);
+    double *cf = reinterpret_cast<double *>(ws + L.cf);
+    double *Hh = reinterpret_cast<double *>(ws + L.hh);
+    double *partials = reinterpret_cast<double *>(ws + L.partials);
+    unsigned *counters = reinterpret_cast<unsigned *>(ws + L.counters);
+    int *status = reinterpret_cast<int *>(ws + L.status);
+    __nv_bfloat16 *hi = uses_bf16(op) ? reinterpret_cast<__nv_bfloat16 *>(ws + L.hi) : nullptr;
+    __nv_bfloat16 *lo = (uses_bf16(op) && op->precision == MFG_PREC_BF16X3)
+                            ? reinterpret_cast<__nv_bfloat16 *>(ws + L.lo)
+                            : nullptr;
+    const double bfb = hi ? (double)n * (double)p * 2.0 * (lo ? 2.0 : 1.0) : 0.0;
+    const int64_t qb = k * ld;
+    const int64_t koff = k, xs = 2 * k + 1;
+    // step 0 as the reference: w = A q_0, h_0 = q_0 . w, u_1 = w - q_0 h_0
+    MFG_LAUNCH(MFG_PROF_APPLY, ab, af, apply_op<T>(op, Q, qb, Wb, ld, p, hi, lo, ld, panel, status, s));
+    MFG_LAUNCH(MFG_PROF_PROJ, 2.0 * vecb, 2.0 * vecb / sizeof(T),
+               launch_proj<T>(Q, qb, ld, 1, Wb, ld, n, p, partials, counters, H, k * k, k, s, status));
+    MFG_LAUNCH(MFG_PROF_SUB, 3.0 * vecb, 4.0 * vecb / sizeof(T),
+               launch_sub<T>(Q, qb, ld, 1, H, k * k, k, Wb, Wb, ld, n, p, true, true, partials,
+                             counters, nu, nullptr, 0, s, status));
+    // qt_1 = u_1 / ||u_1|| (and its bf16 copies when another product follows)
+    MFG_LAUNCH(MFG_PROF_SCALE, 2.0 * vecb + (k > 1 ? bfb : 0.0), vecb / sizeof(T),
+               launch_scale<T>(Wb, ld, n, p, nu, Vt, ld, k > 1 ? hi : nullptr, lo, ld, s));
+    for (int64_t j = 1; j < k; ++j) {
+      const int nc = (int)j;
+      MFG_LAUNCH(MFG_PROF_APPLY, ab, af, apply_op<T>(op, Vt, ld, Wb, ld, p, hi, lo, ld, panel, status, s));
+      // [Q^T qt | Q^T w | qt . w] from one read of the basis
+      MFG_LAUNCH(MFG_PROF_PROJ, (nc + 2.0) * vecb, 4.0 * nc * vecb / sizeof(T),
+                 launch_proj2<T>(Q, qb, ld, nc, Wb, Vt, ld, n, p, partials, counters, X2, xs,
+                                 koff, status, s));
+      // q_j (unnormalised) = qt - Q Q^T qt into row j, w <- w - Q Q^T w
+      MFG_LAUNCH(MFG_PROF_SUBPROJ, (nc + 4.0) * vecb, 4.0 * nc * vecb / sizeof(T),
+                 launch_sub2<T>(Q, qb, ld, nc, X2, xs, koff, Wb, Vt, ld, Q + j * ld, qb, n, p,
+                                partials, counters, dots, status, s));
+      MFG_LAUNCH(MFG_PROF_OTHER, 8.0 * p * (3.0 * k + 2.0 * j), 2.0 * p * j * j,
+                 launch_twosweep_coef((int)j, (int)k, p, X2, koff, dots, H, Hh, nu, cf, status, s));
+      const bool more = j + 1 < k;
+      MFG_LAUNCH(MFG_PROF_SCALE, (more || R ? 4.0 : 2.0) * vecb + (more ? bfb : 0.0),
+                 3.0 * vecb / sizeof(T),
+                 launch_twosweep_finish<T>(Q + j * ld, qb, Wb, ld, n, p, cf,
+                                           (more || R) ? Vt : nullptr, more ? hi : nullptr, lo,
+                                           ld, s));
+    }
+    if (R) {
+      // the reference's last reorthogonalisation: R = nu_k (qt_k - Q Q^T qt_k)
+      const int nc = (int)k;
+      MFG_LAUNCH(MFG_PROF_PROJ, (nc + 1.0) * vecb, 2.0 * nc * vecb / sizeof(T),
+                 launch_proj<T>(Q, qb, ld, nc, Vt, ld, n, p, partials, counters, X2, xs, 1, s, status));
+      MFG_LAUNCH(MFG_PROF_SUB, (nc + 2.0) * vecb, 2.0 * nc * vecb / sizeof(T),
+                 launch_sub<T>(Q, qb, ld, nc, X2, xs, 1, Vt, R, ld, n, p, false, true, partials,
+                               counters, nullptr, nullptr, 0, s, status));
+      MFG_LAUNCH(MFG_PROF_OTHER, 16.0 * p, (double)p, launch_inv(nu, cf, p, s));
+      MFG_LAUNCH(MFG_PROF_SCALE, 2.0 * vecb, vecb / sizeof(T),
+                 launch_scale<T>(R, ld, n, p, cf, R, ld, nullptr, nullptr, ld, s));
+    }
+    return MFG_OK;
+  }
+}
+
 template <typename T>
 static int run_hessenberg(const mfg_operator *op, int64_t k, int64_t p, const T *V, int64_t ld,
                           int reortho, T *Q, double *H, T *R, double *init_len_inv,
@@ -265,6 +367,7 @@ static int run_hessenberg(const mfg_operator *op, int64_t k, int64_t p, const T 
   }
   MFG_LAUNCH(MFG_PROF_SCALE, 2.0 * vecb + bfb, vecb / sizeof(T),
              launch_scale<T>(V, ld, n, p, len0, Q, qb, hi, lo, ld, s));
+  if (reortho == 3) return run_two_sweep<T>(op, k, p, ld, Q, H, R, L, ws, s);
 
   for (int64_t j = 0; j < k; ++j) {
     const T *qj = Q + j * ld;
@@ -784,6 +887,8 @@ const char *mfg_status_string(int status) {
     case MFG_ERR_TIMEOUT: return "a bounded device-side wait timed out";
     case MFG_ERR_SCRATCH_LIMIT:
       return "problem exceeds the fixed 32 MiB scratch of the no-allocation entry point";
+    case MFG_ERR_RETRY:
+      return "two-sweep reorthogonalisation lost accuracy; repeat with the three-sweep form";
     default: return "unknown status";
   }
 }
@@ -923,8 +1028,9 @@ int mfg_hessenberg(const mfg_operator *op, int64_t k, int64_t p, const void *V, 
   if (k < 0 || k > op->n) return MFG_ERR_RANGE;
   if (!V || !aligned16(V) || (k > 0 && (!Q || !H || !aligned16(Q)))) return MFG_ERR_BAD_ARG;
   if (residual && !aligned16(residual)) return MFG_ERR_BAD_ARG;
-  if (reortho < 0 || reortho > 2) return MFG_ERR_BAD_ARG;
-  const WsLayout L = layout(op, k, p, ld);
+  if (reortho < 0 || reortho > 3) return MFG_ERR_BAD_ARG;
+  if (reortho == 3 && !two_sweep_applies(op, k)) reortho = 1;
+  const WsLayout L = layout(op, k, p, ld, reortho == 3);
   if (!workspace || workspace_bytes < L.total) return MFG_ERR_WORKSPACE;
   char *ws = ws_base(workspace);
   cudaStream_t s = as_stream(stream);
@@ -975,16 +1081,17 @@ int mfg_tridiag_quadrature(int64_t k, int64_t p, const double *H, int32_t fun, d
   return MFG_OK;
 }
 
-int mfg_slq(const mfg_operator *op, int64_t k, int64_t p, const void *probes, int64_t ld,
-            int32_t fun, double param, double *values, double *mean_sem, void *Q, double *H,
-            void *workspace, size_t workspace_bytes, void *stream) {
+static int slq_impl(const mfg_operator *op, int64_t k, int64_t p, const void *probes, int64_t ld,
+                    int32_t fun, double param, double *values, double *mean_sem, void *Q,
+                    double *H, bool two, void *workspace, size_t workspace_bytes, void *stream) {
   MFG_TRY(check_op(op));
   MFG_TRY(check_panel(op, p, ld));
   if (k < 0 || k > op->n) return MFG_ERR_RANGE;
   if (k == 0) return MFG_ERR_BAD_ARG;  // e1 of a 0 x 0 matrix does not exist
   if (!probes || !aligned16(probes) || !values) return MFG_ERR_BAD_ARG;
   if (fun < MFG_FUN_LOG || fun > MFG_FUN_POW) return MFG_ERR_BAD_ARG;
-  const WsLayout L = layout(op, k, p, ld);
+  two = two && two_sweep_applies(op, k);
+  const WsLayout L = layout(op, k, p, ld, two);
   if (!workspace || workspace_bytes < L.total) return MFG_ERR_WORKSPACE;
   char *ws = ws_base(workspace);
   cudaStream_t s = as_stream(stream);
@@ -998,8 +1105,8 @@ int mfg_slq(const mfg_operator *op, int64_t k, int64_t p, const void *probes, in
     MFG_TRY(run_hessenberg<double>(op, k, p, (const double *)probes, ld, 1, (double *)Qb, Hb,
                                    nullptr, nullptr, L, ws, s));
   else
-    MFG_TRY(run_hessenberg<float>(op, k, p, (const float *)probes, ld, 1, (float *)Qb, Hb, nullptr,
-                                  nullptr, L, ws, s));
+    MFG_TRY(run_hessenberg<float>(op, k, p, (const float *)probes, ld, two ? 3 : 1, (float *)Qb, Hb,
+                                  nullptr, nullptr, L, ws, s));
   // funm.py:240-241: length^2 * e1^T f(T) e1 with length = ||v||
   MFG_LAUNCH(MFG_PROF_OTHER, 16.0 * p, (double)p, launch_square(len0, scale, p, s));
   MFG_LAUNCH(MFG_PROF_QUAD, 8.0 * p * k * k + 16.0 * p * k, 0.0,
@@ -1008,6 +1115,37 @@ int mfg_slq(const mfg_operator *op, int64_t k, int64_t p, const void *probes, in
                                        reinterpret_cast<double *>(ws + L.fsq), status, s));
   if (mean_sem) MFG_LAUNCH(MFG_PROF_QUAD, 8.0 * p, 3.0 * p, launch_mean_sem(values, p, mean_sem, s));
   return MFG_OK;
+}
+
+int mfg_slq(const mfg_operator *op, int64_t k, int64_t p, const void *probes, int64_t ld,
+            int32_t fun, double param, double *values, double *mean_sem, void *Q, double *H,
+            void *workspace, size_t workspace_bytes, void *stream) {
+  return slq_impl(op, k, p, probes, ld, fun, param, values, mean_sem, Q, H, false, workspace,
+                  workspace_bytes, stream);
+}
+
+size_t mfg_slq_ex_workspace_bytes(const mfg_operator *op, int64_t k, int64_t p, int64_t ld,
+                                  int32_t flags) {
+  if (check_op(op) != MFG_OK || k < 0 || p <= 0 || ld < op->n) return 0;
+  return layout(op, k, p, ld, (flags & MFG_SLQ_TWO_SWEEP) && two_sweep_applies(op, k)).total;
+}
+
+int mfg_slq_ex(const mfg_operator *op, int64_t k, int64_t p, const void *probes, int64_t ld,
+               int32_t fun, double param, double *values, double *mean_sem, void *Q, double *H,
+               int32_t flags, void *workspace, size_t workspace_bytes, void *stream) {
+  if (flags & ~MFG_SLQ_TWO_SWEEP) return MFG_ERR_BAD_ARG;
+  return slq_impl(op, k, p, probes, ld, fun, param, values, mean_sem, Q, H,
+                  (flags & MFG_SLQ_TWO_SWEEP) != 0, workspace, workspace_bytes, stream);
+}
+
+int mfg_workspace_status(const void *workspace, void *stream) {
+  if (!workspace) return MFG_ERR_BAD_ARG;
+  int st = MFG_OK;
+  cudaStream_t s = as_stream(stream);
+  MFG_CUDA_TRY(cudaMemcpyAsync(&st, ws_base(const_cast<void *>(workspace)), sizeof(int),
+                               cudaMemcpyDeviceToHost, s));
+  MFG_CUDA_TRY(cudaStreamSynchronize(s));
+  return st;
 }
 
 static int check_bidiag_ops(const mfg_operator *A, const mfg_operator *At, int64_t p, int64_t ld) {

@@ -33,6 +33,25 @@ int launch_scale(const T *Win, int64_t w_bstride, int64_t n, int64_t p, const do
                  int64_t out_bstride, __nv_bfloat16 *hi, __nv_bfloat16 *lo, int64_t bf_bstride,
                  cudaStream_t s);
 int launch_inv(const double *x, double *y, int64_t p, cudaStream_t s);
+// two-sweep Arnoldi step (lanczos_kernels.cu; float bases, ncols <= kTwoSweepMaxCols)
+constexpr int kTwoSweepMaxCols = 64;
+template <typename T>
+int launch_proj2(const T *Q, int64_t q_bstride, int64_t q_istride, int ncols, const T *Wa,
+                 const T *Wb, int64_t w_bstride, int64_t n, int64_t p, double *partials,
+                 unsigned *counters, double *out, int64_t out_bstride, int64_t koff, int *status,
+                 cudaStream_t s);
+template <typename T>
+int launch_sub2(const T *Q, int64_t q_bstride, int64_t q_istride, int ncols, const double *coef,
+                int64_t c_bstride, int64_t koff, T *Wa, const T *Wb, int64_t w_bstride, T *Wo,
+                int64_t wo_bstride, int64_t n, int64_t p, double *partials, unsigned *counters,
+                double *dots, int *status, cudaStream_t s);
+int launch_twosweep_coef(int j, int k, int64_t p, const double *X2, int64_t koff,
+                         const double *dots, double *H, double *Hh, double *nu, double *cf,
+                         int *status, cudaStream_t s);
+template <typename T>
+int launch_twosweep_finish(T *Qj, int64_t q_bstride, const T *Z, int64_t w_bstride, int64_t n,
+                           int64_t p, const double *cf, T *qt, __nv_bfloat16 *hi,
+                           __nv_bfloat16 *lo, int64_t bf_bstride, cudaStream_t s);
 // conjugate gradients on probe-major panels (lanczos_kernels.cu)
 template <typename T>
 int launch_cg_init(const T *B, T *X, T *R, T *P, int64_t ld, int64_t n, int64_t p,

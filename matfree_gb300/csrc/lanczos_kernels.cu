@@ -519,31 +519,48 @@ __device__ __forceinline__ int64_t cta_of_chunk(int64_t f, int64_t F, int64_t G)
 //   kStreamSubProj  w' = w - Q c (stored), h_i = q_i . w'      (second CGS2 pass)
 //   kStreamProj     h_i = q_i . w                              (first CGS2 pass)
 //   kStreamSubNorm  w' = w - Q c (stored), ||w'||              (final CGS2 update)
-enum : int { kStreamSubProj = 0, kStreamProj = 1, kStreamSubNorm = 2 };
+// and, for the two-sweep Arnoldi step, with two vectors per probe (a = w,
+// b = the second vector):
+//   kStreamProj2    h_i = q_i . b, g_i = q_i . a, a . b
+//   kStreamSub2     b' = b - Q h (stored in a third array), a' = a - Q g
+//                   (stored over a), ||b'||^2, ||a'||^2, b' . a'
+enum : int { kStreamSubProj = 0, kStreamProj = 1, kStreamSubNorm = 2, kStreamProj2 = 3, kStreamSub2 = 4 };
+
+// Per-probe outputs of a pass (the cross-CTA partial-sum stride).
+template <int MAXG, int kMode>
+__host__ __device__ constexpr int stream_nout_max() {
+  return kMode == kStreamProj2 ? 2 * kSPGroup * MAXG + 1
+                               : (kMode == kStreamSub2 ? 3 : (kMode == kStreamSubNorm ? 1 : kSPGroup * MAXG));
+}
 
 template <typename T, int MAXG, bool kHold, int kMode>
 __global__ void __launch_bounds__(kSThreads + 32)
 stream_sweep_kernel(const __grid_constant__ CUtensorMap qmap, const T *__restrict__ Q,
                     int64_t q_bstride, int64_t q_istride, int ncols,
                     const double *__restrict__ coef, int64_t c_bstride, int64_t c_istride,
-                    T *Wv, int64_t w_bstride, int64_t n, int64_t p, int nbuf, int pstride,
+                    T *Wv, int64_t w_bstride, const T *Wv2, int64_t w2_bstride, T *Wo2,
+                    int64_t wo2_bstride, int64_t koff, int64_t n, int64_t p, int nbuf, int pstride,
                     double *__restrict__ partials, unsigned *__restrict__ counters,
                     double *__restrict__ out, int64_t out_bstride, int64_t out_istride,
                     double *__restrict__ out2, int64_t out2_bstride, int *__restrict__ status) {
-  constexpr bool kUpdate = kMode != kStreamProj;   // forms w' = w - Q c
-  constexpr bool kDots = kMode != kStreamSubNorm;  // sums q_i . (w or w')
+  constexpr bool kPair = kMode == kStreamProj2 || kMode == kStreamSub2;  // two vectors a probe
+  constexpr bool kUpdate = kMode == kStreamSubProj || kMode == kStreamSubNorm || kMode == kStreamSub2;
+  constexpr bool kDots = kMode == kStreamSubProj || kMode == kStreamProj || kMode == kStreamProj2;
+  constexpr int kNV = kPair ? 2 : 1;
+  constexpr int kNAcc = kDots ? kSPGroup * MAXG : 1;
   extern __shared__ __align__(128) uint8_t smem[];
   const int ngroups = (ncols + kSPGroup - 1) / kSPGroup;
   const int cpad = ngroups * kSPGroup;
-  const int nout = kDots ? ncols : 1;
-  // ring of nbuf buffers [cpad + 1][kSR]: the chunk's basis rows (zero
-  // columns past ncols), then its rows of w
+  const int nout = kMode == kStreamProj2 || kMode == kStreamSub2 ? stream_nout_max<MAXG, kMode>()
+                                                                 : (kDots ? ncols : 1);
+  // ring of nbuf buffers [cpad + kNV][kSR]: the chunk's basis rows (zero
+  // columns past ncols), then its rows of w (and of the second vector)
   T *bufs = reinterpret_cast<T *>(smem);
-  const size_t bstr = (size_t)(cpad + 1) * kSR;
-  T *s_coef = bufs + nbuf * bstr;  // [cpad], zero past ncols
+  const size_t bstr = (size_t)(cpad + kNV) * kSR;
+  T *s_coef = bufs + nbuf * bstr;  // [kNV][cpad], zero past ncols
   __shared__ __align__(8) uint64_t full_bar[kSMaxBuf];   // copies of the chunk landed
   __shared__ __align__(8) uint64_t empty_bar[kSMaxBuf];  // every row warp is done with it
-  __shared__ double red[kSWarps][kSPGroup * kSMaxGroups];
+  __shared__ double red[kSWarps][kSPGroup * kSMaxGroups + 1];
   __shared__ int s_fail;
   __shared__ int s_last;
 
@@ -581,7 +598,7 @@ stream_sweep_kernel(const __grid_constant__ CUtensorMap qmap, const T *__restric
     // warps have released that buffer's previous chunk; lane c issues
     // copies c, c + 32, ...
     int issued = 0;
-    const int ncopies = full + (ncols - full * kSPGroup) + 1;
+    const int ncopies = full + (ncols - full * kSPGroup) + kNV;
     // position of chunk t: probe b, row chunk c, buffer u used for the
     // (ph)-parity time; advanced without divisions
     int64_t b = f_begin / C, c = f_begin - (f_begin / C) * C;
@@ -600,7 +617,7 @@ stream_sweep_kernel(const __grid_constant__ CUtensorMap qmap, const T *__restric
       const int64_t rows = (n - r0 < kSR) ? (n - r0) : kSR;
       const uint32_t seg_bytes = (uint32_t)(((rows * (int64_t)sizeof(T)) + 15) / 16 * 16);
       const uint32_t bytes = (uint32_t)full * (uint32_t)(kSPGroup * kSR * sizeof(T)) +
-                             seg_bytes * (uint32_t)(ncols - full * kSPGroup + 1);
+                             seg_bytes * (uint32_t)(ncols - full * kSPGroup + kNV);
       if (lane == 0)
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
                          smem_addr(&full_bar[u])),
@@ -617,11 +634,14 @@ stream_sweep_kernel(const __grid_constant__ CUtensorMap qmap, const T *__restric
               "l"(reinterpret_cast<uint64_t>(&qmap)), "r"(smem_addr(&full_bar[u])), "r"(x), "r"(y)
               : "memory");
         } else {
-          // a tail vector, or (last copy) the chunk's rows of w
+          // a tail vector, or (last kNV copies) the chunk's rows of w and of
+          // the second vector
           const int i = full * kSPGroup + (c - full);
-          const bool is_w = c == ncopies - 1;
-          const T *src = is_w ? Wv + b * w_bstride + r0 : Q + b * q_bstride + (int64_t)i * q_istride + r0;
-          T *d = dst + (size_t)(is_w ? cpad : i) * kSR;
+          const int vec = c - (ncopies - kNV);  // 0: w, 1: second vector, < 0: basis
+          const T *src = vec == 0   ? Wv + b * w_bstride + r0
+                         : vec == 1 ? Wv2 + b * w2_bstride + r0
+                                    : Q + b * q_bstride + (int64_t)i * q_istride + r0;
+          T *d = dst + (size_t)(vec >= 0 ? cpad + vec : i) * kSR;
           asm volatile(
               "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
               ::"r"(smem_addr(d)), "l"(reinterpret_cast<uint64_t>(src)), "r"(seg_bytes),
@@ -648,10 +668,15 @@ stream_sweep_kernel(const __grid_constant__ CUtensorMap qmap, const T *__restric
   } else {
     // row warps: thread j owns row j of every chunk
     const int j = threadIdx.x;
-    T acc[kDots ? kSPGroup * MAXG : 1];
+    T acc[kNAcc];
+    T accg[kMode == kStreamProj2 ? kNAcc : 1];  // kStreamProj2: q_i . w (acc: q_i . b)
 #pragma unroll
-    for (int i = 0; i < (kDots ? kSPGroup * MAXG : 1); ++i) acc[i] = (T)0;
-    double nrm = 0.0;  // ||w'||^2 over this thread's rows (kStreamSubNorm)
+    for (int i = 0; i < kNAcc; ++i) acc[i] = (T)0;
+#pragma unroll
+    for (int i = 0; i < (kMode == kStreamProj2 ? kNAcc : 1); ++i) accg[i] = (T)0;
+    T cross = (T)0;    // a . b over this thread's rows (kStreamProj2)
+    double nrm = 0.0;  // ||w'||^2 over this thread's rows (kStreamSubNorm, kStreamSub2: ||b'||^2)
+    double nrm2 = 0.0, dot2 = 0.0;  // kStreamSub2: ||a'||^2, b' . a'
     int64_t b = f_begin / C, c = f_begin - (f_begin / C) * C;
     int u = 0;
     uint32_t ph = 0;
@@ -662,8 +687,10 @@ stream_sweep_kernel(const __grid_constant__ CUtensorMap qmap, const T *__restric
           // a new probe: its coefficients (the row warps are past every read
           // of the previous ones)
           row_warps_sync();
-          for (int i = j; i < cpad; i += kSThreads)
+          for (int i = j; i < cpad; i += kSThreads) {
             s_coef[i] = i < ncols ? (T)coef[b * c_bstride + i * c_istride] : (T)0;
+            if constexpr (kPair) s_coef[cpad + i] = i < ncols ? (T)coef[b * c_bstride + koff + i] : (T)0;
+          }
           row_warps_sync();
         }
       }
@@ -683,7 +710,26 @@ stream_sweep_kernel(const __grid_constant__ CUtensorMap qmap, const T *__restric
       const int rows = (int)((n - r0 < kSR) ? (n - r0) : kSR);
       T qv[kHold ? kSPGroup * MAXG : 1];
       T w = ready ? buf[(size_t)cpad * kSR] : (T)0;
-      if constexpr (kUpdate) {
+      T w2v = (kPair && ready) ? buf[(size_t)(cpad + 1) * kSR] : (T)0;  // second vector
+      if constexpr (kMode == kStreamSub2) {
+        // b' = b - Q h and a' = a - Q g over this thread's row
+        T a0 = w, a1 = (T)0, b0 = w2v, b1 = (T)0;
+#pragma unroll
+        for (int g = 0; g < MAXG; ++g)
+          if (ready && g < ngroups) {
+#pragma unroll
+            for (int e = 0; e < kSPGroup; e += 2) {
+              const int i = g * kSPGroup + e;
+              const T q0 = buf[(size_t)i * kSR], q1 = buf[(size_t)(i + 1) * kSR];
+              b0 = fma(-q0, s_coef[i], b0);
+              b1 = fma(-q1, s_coef[i + 1], b1);
+              a0 = fma(-q0, s_coef[cpad + i], a0);
+              a1 = fma(-q1, s_coef[cpad + i + 1], a1);
+            }
+          }
+        w = a0 + a1;
+        w2v = b0 + b1;
+      } else if constexpr (kUpdate) {
         // w' = w - Q c over this thread's row; four interleaved sums shorten
         // the dependent chain
         T w0 = w, w1 = (T)0, w2 = (T)0, w3 = (T)0;
@@ -716,7 +762,26 @@ stream_sweep_kernel(const __grid_constant__ CUtensorMap qmap, const T *__restric
           const T w2 = w * w;
           nrm += (double)w2;
         }
-        if constexpr (kDots) {
+        if constexpr (kMode == kStreamSub2) {
+          Wo2[b * wo2_bstride + r0 + j] = w2v;
+          nrm += (double)(w2v * w2v);
+          nrm2 += (double)(w * w);
+          dot2 += (double)(w2v * w);
+        }
+        if constexpr (kMode == kStreamProj2) {
+#pragma unroll
+          for (int g = 0; g < MAXG; ++g)
+            if (g < ngroups) {
+#pragma unroll
+              for (int e = 0; e < kSPGroup; ++e) {
+                const int i = g * kSPGroup + e;
+                const T q = buf[(size_t)i * kSR];
+                acc[i] = fma(q, w2v, acc[i]);
+                accg[i] = fma(q, w, accg[i]);
+              }
+            }
+          cross = fma(w, w2v, cross);
+        } else if constexpr (kDots) {
 #pragma unroll
           for (int g = 0; g < MAXG; ++g)
             if (g < ngroups) {
@@ -737,31 +802,63 @@ stream_sweep_kernel(const __grid_constant__ CUtensorMap qmap, const T *__restric
       if (t + 1 == nt || c + 1 == C) {
         if constexpr (kDots) {
           // per-thread float sums -> warp butterfly -> fixed-order warp sum
-          warp_xsum<T, kSPGroup * MAXG>(acc, lane);
-          constexpr int kPer = (kSPGroup * MAXG) / 32 > 0 ? (kSPGroup * MAXG) / 32 : 1;
-          constexpr int kDup = (kSPGroup * MAXG) >= 32 ? 1 : 32 / (kSPGroup * MAXG);
+          warp_xsum<T, kNAcc>(acc, lane);
+          constexpr int kPer = kNAcc / 32 > 0 ? kNAcc / 32 : 1;
+          constexpr int kDup = kNAcc >= 32 ? 1 : 32 / kNAcc;
           if ((lane & (kDup - 1)) == 0) {
 #pragma unroll
-            for (int i = 0; i < kPer; ++i) red[warp][xsum_index<kSPGroup * MAXG>(lane, i)] = (double)acc[i];
+            for (int i = 0; i < kPer; ++i) red[warp][xsum_index<kNAcc>(lane, i)] = (double)acc[i];
           }
 #pragma unroll
-          for (int i = 0; i < kSPGroup * MAXG; ++i) acc[i] = (T)0;
+          for (int i = 0; i < kNAcc; ++i) acc[i] = (T)0;
+          if constexpr (kMode == kStreamProj2) {
+            // second half of the outputs: q_i . w, then a . b
+            warp_xsum<T, kNAcc>(accg, lane);
+            if ((lane & (kDup - 1)) == 0) {
+#pragma unroll
+              for (int i = 0; i < kPer; ++i) red[warp][kNAcc + xsum_index<kNAcc>(lane, i)] = (double)accg[i];
+            }
+#pragma unroll
+            for (int i = 0; i < kNAcc; ++i) accg[i] = (T)0;
+            const double v = warp_sum((double)cross);
+            if (lane == 0) red[warp][2 * kNAcc] = v;
+            cross = (T)0;
+          }
+        } else if constexpr (kMode == kStreamSub2) {
+          const double v0 = warp_sum(nrm), v1 = warp_sum(nrm2), v2 = warp_sum(dot2);
+          if (lane == 0) {
+            red[warp][0] = v0;
+            red[warp][1] = v1;
+            red[warp][2] = v2;
+          }
+          nrm = nrm2 = dot2 = 0.0;
         } else {
           const double v = warp_sum(nrm);
           if (lane == 0) red[warp][0] = v;
           nrm = 0.0;
         }
         row_warps_sync();
-        double h = 0.0;
-        if (j < nout) {
+        // thread j reduces outputs j and j + kSThreads (at most nout <= 2 kSThreads + 1)
+        constexpr int kOut = kMode == kStreamProj2 ? 2 : 1;
+        double h[kOut];
 #pragma unroll
-          for (int q = 0; q < kSWarps; ++q) h += red[q][j];
+        for (int o = 0; o < kOut; ++o) {
+          const int v = j + o * kSThreads;
+          h[o] = 0.0;
+          if (v < nout) {
+#pragma unroll
+            for (int q = 0; q < kSWarps; ++q) h[o] += red[q][v];
+          }
         }
         const int64_t first = cta_of_chunk(b * C, F, G), last = cta_of_chunk(b * C + C - 1, F, G);
         bool emit = first == last;
         if (!emit) {
           const int64_t seg = (int64_t)blockIdx.x - first;
-          if (j < nout) partials[(b * pstride + seg) * nout + j] = h;
+#pragma unroll
+          for (int o = 0; o < kOut; ++o) {
+            const int v = j + o * kSThreads;
+            if (v < nout) partials[(b * pstride + seg) * nout + v] = h[o];
+          }
           __threadfence();
           row_warps_sync();
           if (j == 0) {
@@ -772,21 +869,40 @@ stream_sweep_kernel(const __grid_constant__ CUtensorMap qmap, const T *__restric
           if (s_last) {
             __threadfence();
             emit = true;
-            if (j < nout) {
-              h = 0.0;
-              for (int64_t q = 0; q <= last - first; ++q)
-                h += __ldcg(&partials[(b * pstride + q) * nout + j]);
+#pragma unroll
+            for (int o = 0; o < kOut; ++o) {
+              const int v = j + o * kSThreads;
+              if (v < nout) {
+                h[o] = 0.0;
+                for (int64_t q = 0; q <= last - first; ++q)
+                  h[o] += __ldcg(&partials[(b * pstride + q) * nout + v]);
+              }
             }
             if (j == 0) counters[b] = 0u;
           }
         }
-        if (emit && j < nout) {
-          if constexpr (kMode == kStreamSubNorm) {
-            const double nv = sqrt(h);
-            out[b * out_bstride] = nv;
-            if (out2) out2[b * out2_bstride] = nv;
-          } else {
-            out[b * out_bstride + j * out_istride] = h;
+        if (emit) {
+#pragma unroll
+          for (int o = 0; o < kOut; ++o) {
+            const int v = j + o * kSThreads;
+            if (v >= nout) continue;
+            if constexpr (kMode == kStreamSubNorm) {
+              const double nv = sqrt(h[o]);
+              out[b * out_bstride] = nv;
+              if (out2) out2[b * out2_bstride] = nv;
+            } else if constexpr (kMode == kStreamSub2) {
+              out[b * out_bstride + v] = h[o];
+            } else if constexpr (kMode == kStreamProj2) {
+              constexpr int kHalf = kSPGroup * MAXG;
+              if (v == 2 * kHalf) {
+                out[b * out_bstride + 2 * koff] = h[o];
+              } else {
+                const int half = v / kHalf, i = v - half * kHalf;
+                if (i < ncols) out[b * out_bstride + half * koff + i] = h[o];
+              }
+            } else {
+              out[b * out_bstride + v * out_istride] = h[o];
+            }
           }
         }
         // red and s_last are reused at this CTA's next probe
@@ -806,9 +922,9 @@ stream_sweep_kernel(const __grid_constant__ CUtensorMap qmap, const T *__restric
 }
 
 template <typename T>
-static size_t stream_sweep_smem(int ncols, int nbuf) {
+static size_t stream_sweep_smem(int ncols, int nbuf, int nv = 1) {
   const int cpad = (ncols + kSPGroup - 1) / kSPGroup * kSPGroup;
-  return (size_t)nbuf * (cpad + 1) * kSR * sizeof(T) + (size_t)cpad * sizeof(T);
+  return (size_t)nbuf * (cpad + nv) * kSR * sizeof(T) + (size_t)nv * cpad * sizeof(T);
 }
 
 // Largest vector count of the streamed sweeps: 128 floats, 64 doubles (the
@@ -818,11 +934,11 @@ template <typename T> constexpr int stream_sweep_max_cols() { return sizeof(T) =
 // Ring depth: as many buffers (2..8) as fit in ~110 KB, so that two CTAs
 // share an SM; 0 if the sweep does not apply.
 template <typename T>
-static int stream_sweep_buffers(int ncols) {
+static int stream_sweep_buffers(int ncols, int nv = 1) {
   if (ncols < 1 || ncols > stream_sweep_max_cols<T>()) return 0;
   int nb = kSMaxBuf;
-  while (nb > 2 && stream_sweep_smem<T>(ncols, nb) > 110 * 1024) --nb;
-  return stream_sweep_smem<T>(ncols, nb) <= 220 * 1024 ? nb : 0;
+  while (nb > 2 && stream_sweep_smem<T>(ncols, nb, nv) > 110 * 1024) --nb;
+  return stream_sweep_smem<T>(ncols, nb, nv) <= 220 * 1024 ? nb : 0;
 }
 
 struct StreamArgs {
@@ -840,13 +956,20 @@ struct StreamArgs {
   double *out2;
   int64_t out2_bstride;
   int *status;
+  // two-vector passes: the second vector, where its update goes, and the
+  // offset of the second coefficient / output block of a probe
+  const void *Wv2 = nullptr;
+  int64_t w2_bstride = 0;
+  void *Wo2 = nullptr;
+  int64_t wo2_bstride = 0, koff = 0;
 };
 
 template <typename T, int MAXG, bool kHold, int kMode>
 static int launch_stream_sweep_t(const StreamArgs &a, cudaStream_t s) {
-  const int nbuf = stream_sweep_buffers<T>(a.ncols);
+  constexpr int nv = (kMode == kStreamProj2 || kMode == kStreamSub2) ? 2 : 1;
+  const int nbuf = stream_sweep_buffers<T>(a.ncols, nv);
   if (nbuf < 2) return MFG_ERR_UNSUPPORTED;
-  const size_t smem = stream_sweep_smem<T>(a.ncols, nbuf);
+  const size_t smem = stream_sweep_smem<T>(a.ncols, nbuf, nv);
   if (a.q_istride <= 0 || a.q_bstride % a.q_istride != 0) return MFG_ERR_BAD_ARG;
   auto kern = stream_sweep_kernel<T, MAXG, kHold, kMode>;
   // The default dynamic limit is 48 KB minus the kernel's static shared
@@ -855,7 +978,7 @@ static int launch_stream_sweep_t(const StreamArgs &a, cudaStream_t s) {
     MFG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   // resident CTAs per SM for this vector count (cached: the answer depends
   // only on the shared-memory size, i.e. on ncols)
-  static int per_sm_cache[129];
+  static int per_sm_cache[129];  // one cache per template instance
   static int sms = 0;
   if (sms == 0) {
     int dev = 0;
@@ -890,13 +1013,27 @@ static int launch_stream_sweep_t(const StreamArgs &a, cudaStream_t s) {
     return MFG_ERR_CUDA;
   kern<<<(unsigned)G, kSThreads + 32, smem, s>>>(
       qmap, static_cast<const T *>(a.Q), a.q_bstride, a.q_istride, a.ncols, a.coef, a.c_bstride,
-      a.c_istride, static_cast<T *>(a.Wv), a.w_bstride, a.n, a.p, nbuf, pstride, a.partials,
-      a.counters, a.out, a.out_bstride, a.out_istride, a.out2, a.out2_bstride, a.status);
+      a.c_istride, static_cast<T *>(a.Wv), a.w_bstride, static_cast<const T *>(a.Wv2),
+      a.w2_bstride, static_cast<T *>(a.Wo2), a.wo2_bstride, a.koff, a.n, a.p, nbuf, pstride,
+      a.partials, a.counters, a.out, a.out_bstride, a.out_istride, a.out2, a.out2_bstride,
+      a.status);
   return MFG_LAUNCH_STATUS();
 }
 
 template <typename T, int kMode>
 static int launch_stream_sweep(const StreamArgs &a, cudaStream_t s) {
+  if constexpr (kMode == kStreamProj2 || kMode == kStreamSub2) {
+    // two vectors: float bases of up to 64 vectors (the per-thread sums of
+    // both vectors stay in registers), no register-held basis values
+    if constexpr (sizeof(T) != 4) {
+      return MFG_ERR_UNSUPPORTED;
+    } else {
+      if (a.ncols < 1 || a.ncols > kTwoSweepMaxCols) return MFG_ERR_UNSUPPORTED;
+      if (a.ncols <= 8) return launch_stream_sweep_t<T, 1, false, kMode>(a, s);
+      if (a.ncols <= 32) return launch_stream_sweep_t<T, 4, false, kMode>(a, s);
+      return launch_stream_sweep_t<T, 8, false, kMode>(a, s);
+    }
+  }
   if (stream_sweep_buffers<T>(a.ncols) == 0) return MFG_ERR_UNSUPPORTED;
   // loops (and, for dot products, register sums) sized to the vector count:
   // 8, 32, 64 or 128; in the two-pass form up to 64 (32 doubles) basis
@@ -1195,6 +1332,239 @@ int launch_cg_direction(T *P, const T *R, int64_t ld, int64_t n, int64_t p, cons
       P, R, ld, n, rs, rs_next, thr, hi, lo);
   return MFG_LAUNCH_STATUS();
 }
+
+// ---------------------------------------------------------------------------
+// Two-sweep Arnoldi step (reortho = full, float bases of up to 64 vectors).
+//
+// The reference's step j (decomp.py:454-477) reads the basis three times:
+// h = Q^T w, w' = w - Q h, w'' = w' - Q (Q^T w'), ||w''||.  Here the second
+// projection of step j-1 is done in step j, over the same two reads of the
+// basis as step j's own first projection.  The operator is applied to
+// qt_j = u_j / nu_j, u_j = w'_{j-1} (first-projected, not yet
+// reorthogonalised), and A q_j follows from the Arnoldi relation
+// A Q_{j-1} = Q_j Hh (Hh: the full coefficients h + h2 and beta):
+//   q_j = (u_j - Q h2) / beta,   A q_j = (nu_j A qt_j - Q_j Hh h2) / beta,
+//   h_j = Q_j^T A q_j = (nu_j [g; q_j . A qt_j] - Hh h2) / beta,
+//   w'_j = (I - Q_j Q_j^T) A q_j = (nu_j / beta) (I - Q_j Q_j^T) A qt_j.
+// In exact arithmetic H, beta and the basis equal the reference's.  The
+// rounding of A q_j grows with nu_j / beta_{j-1}, i.e. with the size of the
+// second projection; when ||Q^T qt_j|| exceeds 0.1 (a vector that one
+// projection left largely inside the basis, near an invariant subspace) the
+// step raises MFG_ERR_RETRY and the caller repeats the solve with the
+// three-sweep form.
+// ---------------------------------------------------------------------------
+
+// a = w (per probe rows of w_bstride), b = qt: out[b] = [Q^T qt (k) | Q^T w (k) | qt . w]
+template <typename T>
+int launch_proj2(const T *Q, int64_t q_bstride, int64_t q_istride, int ncols, const T *Wa,
+                 const T *Wb, int64_t w_bstride, int64_t n, int64_t p, double *partials,
+                 unsigned *counters, double *out, int64_t out_bstride, int64_t koff, int *status,
+                 cudaStream_t s) {
+  if (ncols <= 0 || p <= 0) return MFG_OK;
+  StreamArgs a{Q,        q_bstride,   q_istride, ncols,   nullptr,  0,       0,
+               const_cast<T *>(Wa), w_bstride, n,       p,        partials, counters,
+               out,      out_bstride, 1,         nullptr, 0,        status};
+  a.Wv2 = Wb;
+  a.w2_bstride = w_bstride;
+  a.koff = koff;
+  return launch_stream_sweep<T, kStreamProj2>(a, s);
+}
+
+// Wa <- Wa - Q g (coef + koff), Wo <- Wb - Q h (coef); dots[b] = (||Wo||^2, ||Wa||^2, Wo . Wa)
+template <typename T>
+int launch_sub2(const T *Q, int64_t q_bstride, int64_t q_istride, int ncols, const double *coef,
+                int64_t c_bstride, int64_t koff, T *Wa, const T *Wb, int64_t w_bstride, T *Wo,
+                int64_t wo_bstride, int64_t n, int64_t p, double *partials, unsigned *counters,
+                double *dots, int *status, cudaStream_t s) {
+  if (ncols <= 0 || p <= 0) return MFG_OK;
+  StreamArgs a{Q,  q_bstride, q_istride, ncols,   coef,     c_bstride, 1,
+               Wa, w_bstride, n,         p,       partials, counters,  dots,
+               3,  1,         nullptr,   0,       status};
+  a.Wv2 = Wb;
+  a.w2_bstride = w_bstride;
+  a.Wo2 = Wo;
+  a.wo2_bstride = wo_bstride;
+  a.koff = koff;
+  return launch_stream_sweep<T, kStreamSub2>(a, s);
+}
+
+// One warp per probe: the coefficient algebra of step j >= 1 (see above).
+// X2: [Q^T qt (j) | Q^T w (j) at koff | qt . w at 2 koff], dots: (||b'||^2,
+// ||z||^2, b' . z) with b' = qt - Q Q^T qt, z = w - Q Q^T w.  Writes H row/col
+// entries of the reference's H, the full coefficients Hh ((k + 1) x k), the
+// next scale nu and the finish coefficients cf = (1/rho, 1/s, qw/(rho s)).
+// Hh is stored column-major ((k + 1) rows a column) so that a column update
+// and the product Hh h2 read and write consecutive words across the lanes.
+__global__ void twosweep_coef_kernel(int j, int k, int64_t p, const double *__restrict__ X2,
+                                     int64_t koff, const double *__restrict__ dots,
+                                     double *__restrict__ H, double *__restrict__ Hh,
+                                     double *__restrict__ nu, double *__restrict__ cf,
+                                     int *__restrict__ status) {
+  const int lane = threadIdx.x & 31;
+  const int64_t b = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (b >= p) return;  // warp-uniform
+  const double *x = X2 + b * (2 * koff + 1);
+  double *Hb = H + b * (int64_t)k * k;
+  double *Hhb = Hh + b * (int64_t)(k + 1) * k;  // column-major: column l at Hhb + l (k + 1)
+  const int64_t ld = k + 1;
+  // every input first, in one round of independent loads; lane owns rows
+  // lane, lane + 32 and lane + 64 (j <= 64)
+  const double nb = dots[b * 3], nz = dots[b * 3 + 1], bz = dots[b * 3 + 2];
+  const double c = x[2 * koff], nuj = nu[b];
+  const bool r0 = lane < j, r1 = lane + 32 < j;
+  const double hq0 = r0 ? x[lane] : 0.0, hq1 = r1 ? x[lane + 32] : 0.0;
+  const double g0 = r0 ? x[koff + lane] : 0.0, g1 = r1 ? x[koff + lane + 32] : 0.0;
+  const double hp0 = r0 ? Hb[(int64_t)lane * k + (j - 1)] : 0.0;
+  const double hp1 = r1 ? Hb[(int64_t)(lane + 32) * k + (j - 1)] : 0.0;
+  const double hh = warp_sum(fma(hq0, hq0, hq1 * hq1));
+  const double hg = warp_sum(fma(hq0, g0, hq1 * g1));
+  const double rho = sqrt(nb);   // ||w''_{j-1}|| / nu_j
+  const double beta = nuj * rho;
+  // column j-1 of Hh (the reference's h_{j-1} plus the second projection,
+  // beta below it), kept in registers for the product below
+  const double cj0 = r0 ? hp0 + nuj * hq0 : (lane == j ? beta : 0.0);
+  const double cj1 = r1 ? hp1 + nuj * hq1 : (lane + 32 == j ? beta : 0.0);
+  const double cj2 = lane + 64 == j ? beta : 0.0;
+  double *col = Hhb + (int64_t)(j - 1) * ld;
+  if (lane <= j) col[lane] = cj0;
+  if (lane + 32 <= j) col[lane + 32] = cj1;
+  if (lane + 64 <= j) col[lane + 64] = cj2;
+  if (lane == 0) Hb[(int64_t)j * k + (j - 1)] = beta;
+  const double qw = (c - hg) / rho;  // q_j . A qt_j
+  if (j < k) {
+    // m = Hh[0:j+1, 0:j] hq: all lanes walk the same columns (hq_l broadcast
+    // by shuffle), eight columns of loads in flight; entries below the
+    // subdiagonal (never written) are masked
+    double m0 = 0.0, m1 = 0.0, m2 = 0.0;
+    for (int l0 = 0; l0 < j - 1; l0 += 8) {
+      double a0[8], a1[8], a2[8];
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        const int l = l0 + t;
+        const double *cl = Hhb + (int64_t)l * ld;
+        const bool ok = l < j - 1;
+        a0[t] = ok && lane <= l + 1 ? cl[lane] : 0.0;
+        a1[t] = ok && lane + 32 <= l + 1 ? cl[lane + 32] : 0.0;
+        a2[t] = ok && lane + 64 <= l + 1 ? cl[lane + 64] : 0.0;
+      }
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        const int l = l0 + t;
+        const double hv = __shfl_sync(0xffffffffu, l < 32 ? hq0 : hq1, l & 31);
+        m0 = fma(a0[t], hv, m0);
+        m1 = fma(a1[t], hv, m1);
+        m2 = fma(a2[t], hv, m2);
+      }
+    }
+    const double hv = __shfl_sync(0xffffffffu, j - 1 < 32 ? hq0 : hq1, (j - 1) & 31);
+    m0 = fma(cj0, hv, m0);
+    m1 = fma(cj1, hv, m1);
+    m2 = fma(cj2, hv, m2);
+    // h_j = (nu [g; qw] - m) / beta into column j of H
+    if (lane <= j) Hb[(int64_t)lane * k + j] = nuj * ((r0 ? g0 : qw) - m0) / beta;
+    if (lane + 32 <= j) Hb[(int64_t)(lane + 32) * k + j] = nuj * ((r1 ? g1 : qw) - m1) / beta;
+    if (lane + 64 <= j) Hb[(int64_t)(lane + 64) * k + j] = nuj * (qw - m2) / beta;
+  }
+  if (lane == 0) {
+    if (hh > 0.01 * (hh + nb) && status) atomicExch(status, (int)MFG_ERR_RETRY);
+    // y = z - q_j qw, ||y||^2 = ||z||^2 - 2 qw (q_j . z) + qw^2
+    const double qz = bz / rho;
+    const double s2 = nz - 2.0 * qw * qz + qw * qw;
+    const double sy = s2 > 1e-12 * nz ? sqrt(s2) : sqrt(nz);
+    nu[b] = sy / rho;  // u_{j+1} = y / rho = nu_{j+1} qt_{j+1}
+    cf[b * 4] = 1.0 / rho;
+    cf[b * 4 + 1] = 1.0 / sy;
+    cf[b * 4 + 2] = qw / (rho * sy);
+  }
+}
+
+// End of step j: q_j = b' / rho in place; qt_{j+1} = z / s - b' qw / (rho s)
+// (float copy and bf16 hi/lo) unless qt is null.
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+twosweep_finish_kernel(T *__restrict__ Qj, int64_t q_bstride, const T *__restrict__ Z,
+                       int64_t w_bstride, int64_t n, const double *__restrict__ cf,
+                       T *__restrict__ qt, __nv_bfloat16 *__restrict__ hi,
+                       __nv_bfloat16 *__restrict__ lo, int64_t bf_bstride) {
+  constexpr int W = Vec<T>::width;
+  const int64_t c = blockIdx.x;
+  const int64_t b = blockIdx.y;
+  const T t1 = (T)cf[b * 4], cz = (T)cf[b * 4 + 1], cb = (T)cf[b * 4 + 2];
+  T bv[kVPT][W], zv[kVPT][W];
+  load_chunk<T>(Qj + b * q_bstride, n, c, bv);
+  if (qt) load_chunk<T>(Z + b * w_bstride, n, c, zv);
+#pragma unroll
+  for (int e = 0; e < kVPT; ++e)
+#pragma unroll
+    for (int u = 0; u < W; ++u) {
+      const T bb = bv[e][u];
+      bv[e][u] = bb * t1;
+      if (qt) zv[e][u] = zv[e][u] * cz - bb * cb;
+    }
+  store_chunk<T>(Qj + b * q_bstride, n, c, bv);
+  if (!qt) return;
+  store_chunk<T>(qt + b * w_bstride, n, c, zv);
+  if (hi == nullptr) return;
+#pragma unroll
+  for (int e = 0; e < kVPT; ++e) {
+    const int64_t r = c * chunk_rows<T>() + ((int64_t)e * kThreads + threadIdx.x) * W;
+    if (r >= n) continue;
+    __nv_bfloat16 h[W], l[W];
+#pragma unroll
+    for (int u = 0; u < W; ++u) {
+      const float xv = (float)zv[e][u];
+      h[u] = __float2bfloat16_rn(xv);
+      l[u] = __float2bfloat16_rn(xv - __bfloat162float(h[u]));
+    }
+    if constexpr (W == 4) {
+      uint2 hv, lv;
+      hv.x = (uint32_t)__bfloat16_as_ushort(h[0]) | ((uint32_t)__bfloat16_as_ushort(h[1]) << 16);
+      hv.y = (uint32_t)__bfloat16_as_ushort(h[2]) | ((uint32_t)__bfloat16_as_ushort(h[3]) << 16);
+      lv.x = (uint32_t)__bfloat16_as_ushort(l[0]) | ((uint32_t)__bfloat16_as_ushort(l[1]) << 16);
+      lv.y = (uint32_t)__bfloat16_as_ushort(l[2]) | ((uint32_t)__bfloat16_as_ushort(l[3]) << 16);
+      *reinterpret_cast<uint2 *>(hi + b * bf_bstride + r) = hv;
+      if (lo) *reinterpret_cast<uint2 *>(lo + b * bf_bstride + r) = lv;
+    } else {
+#pragma unroll
+      for (int u = 0; u < W; ++u) {
+        hi[b * bf_bstride + r + u] = h[u];
+        if (lo) lo[b * bf_bstride + r + u] = l[u];
+      }
+    }
+  }
+}
+
+int launch_twosweep_coef(int j, int k, int64_t p, const double *X2, int64_t koff,
+                         const double *dots, double *H, double *Hh, double *nu, double *cf,
+                         int *status, cudaStream_t s) {
+  if (p <= 0) return MFG_OK;
+  twosweep_coef_kernel<<<(unsigned)ceil_div(p, 4), 128, 0, s>>>(j, k, p, X2, koff, dots, H, Hh,
+                                                                nu, cf, status);
+  return MFG_LAUNCH_STATUS();
+}
+
+template <typename T>
+int launch_twosweep_finish(T *Qj, int64_t q_bstride, const T *Z, int64_t w_bstride, int64_t n,
+                           int64_t p, const double *cf, T *qt, __nv_bfloat16 *hi,
+                           __nv_bfloat16 *lo, int64_t bf_bstride, cudaStream_t s) {
+  if (p <= 0) return MFG_OK;
+  if (p > 65535) return MFG_ERR_UNSUPPORTED;
+  dim3 grid((unsigned)num_chunks<T>(n), (unsigned)p);
+  twosweep_finish_kernel<T><<<grid, kThreads, 0, s>>>(Qj, q_bstride, Z, w_bstride, n, cf, qt, hi,
+                                                      lo, bf_bstride);
+  return MFG_LAUNCH_STATUS();
+}
+
+template int launch_proj2<float>(const float *, int64_t, int64_t, int, const float *,
+                                 const float *, int64_t, int64_t, int64_t, double *, unsigned *,
+                                 double *, int64_t, int64_t, int *, cudaStream_t);
+template int launch_sub2<float>(const float *, int64_t, int64_t, int, const double *, int64_t,
+                                int64_t, float *, const float *, int64_t, float *, int64_t,
+                                int64_t, int64_t, double *, unsigned *, double *, int *,
+                                cudaStream_t);
+template int launch_twosweep_finish<float>(float *, int64_t, const float *, int64_t, int64_t,
+                                           int64_t, const double *, float *, __nv_bfloat16 *,
+                                           __nv_bfloat16 *, int64_t, cudaStream_t);
 
 #define MFG_INST(T)                                                                          \
   template int launch_cg_init<T>(const T *, T *, T *, T *, int64_t, int64_t, int64_t,         \

@@ -304,10 +304,10 @@ __device__ bool dc_secular_root(const double *P, const double *ZZ, int mk, int j
   if (mk == 1) {
     x = rho * zzj;
   } else if (last) {
-    const double c = fmid - zzj / (P[j] - xma) - zzjm / (P[j - 1] - xma);
+    const double c = fmid - zzj * rcp_nr(P[j] - xma) - zzjm * rcp_nr(P[j - 1] - xma);
     x = c > 0.0 ? xm + dc_quad_step_right(c, P0 - xm, P1 - xm, zzjm, zzj, fmid) : xm;
   } else {
-    const double c = fmid - zzj / (P[j] - xma) - zzj1 / (P[j + 1] - xma);
+    const double c = fmid - zzj * rcp_nr(P[j] - xma) - zzj1 * rcp_nr(P[j + 1] - xma);
     x = dc_quad_root(c, P1, P2, zzj, zzj1);
   }
   if (!(lo < x && x < hi)) x = xm;
@@ -333,9 +333,9 @@ __device__ bool dc_secular_root(const double *P, const double *ZZ, int mk, int j
     const double A = P1 - x;
     const double B = P2 - x;
     const double A0 = P0 - x;
-    const double tj = zzj / A;
-    const double tj1 = last ? 0.0 : zzj1 / B;
-    const double tjm = two_below ? zzjm / A0 : 0.0;
+    const double tj = zzj * rcp_nr(A);
+    const double tj1 = last ? 0.0 : zzj1 * rcp_nr(B);
+    const double tjm = two_below ? zzjm * rcp_nr(A0) : 0.0;
     const double f = ir + rs + tj + tj1 + tjm;
     const double sab = ab + fabs(tj) + fabs(tj1) + fabs(tjm);
     if (f > 0.0)
@@ -456,7 +456,7 @@ __device__ bool dc_merge_roots(const DcArrays &Ar, int k, int s, int nm) {
   return ok;
 }
 
-__global__ void __launch_bounds__(kDcMaxThreads)
+__global__ void __launch_bounds__(kDcMaxThreads, 1)
     tridiag_dc_kernel(int k, int64_t p, const double *__restrict__ H, int fun, double param,
                       const double *__restrict__ scale, double *__restrict__ values,
                       double *__restrict__ eigvals, double *__restrict__ first_sq,

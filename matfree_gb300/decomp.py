@@ -45,6 +45,10 @@ _WS = Workspace()
 def run_hessenberg(op, k: int, V: torch.Tensor, *, reortho: str = "full", workspace=None):
     """Batched Arnoldi over the rows of V (p, n) on the GPU.
 
+    ``reortho``: "full" (Gram-Schmidt twice, three reads of the basis per
+    step), "full-two-sweep" (the same in two reads, repeated as "full" when
+    the device reports a step near an invariant subspace), "none", or
+    "lanczos" (the three-term recurrence).
     Returns (Q (p, k, n), H (p, k, k) float64, residual (p, n), 1/||v|| (p,)).
     """
     require_cuda(V, "vectors")
@@ -60,9 +64,10 @@ def run_hessenberg(op, k: int, V: torch.Tensor, *, reortho: str = "full", worksp
     c = torch.zeros((p,), dtype=torch.float64, device=V.device)
     s = op.c_struct()
     lib = _lib.lib()
-    nbytes = lib.mfg_slq_workspace_bytes(ctypes.byref(s), k, p, ld)
+    mode = {"none": 0, "full": 1, "lanczos": 2, "full-two-sweep": 3}[reortho]
+    flags = _lib.MFG_SLQ_TWO_SWEEP if mode == 3 else 0
+    nbytes = lib.mfg_slq_ex_workspace_bytes(ctypes.byref(s), k, p, ld, flags)
     ws, wsb = (workspace or _WS).get(nbytes, V.device)
-    mode = {"none": 0, "full": 1, "lanczos": 2}[reortho]
     st = lib.mfg_hessenberg(ctypes.byref(s), k, p, ctypes.c_void_p(panel.data_ptr()), ld, mode,
                             ctypes.c_void_p(Q.data_ptr() if k > 0 else 0),
                             ctypes.c_void_p(H.data_ptr() if k > 0 else 0),
@@ -73,6 +78,12 @@ def run_hessenberg(op, k: int, V: torch.Tensor, *, reortho: str = "full", worksp
         op.error = None
         raise err
     _lib.check(st, "mfg_hessenberg")
+    if mode == 3:
+        # the two-sweep step asks for the three-sweep form near an invariant subspace
+        dst = lib.mfg_workspace_status(ws, stream_ptr())
+        if dst == _lib.MFG_ERR_RETRY:
+            return run_hessenberg(op, k, V, reortho="full", workspace=workspace)
+        _lib.check(dst, "mfg_hessenberg (device status)")
     return Q[:, :, :n], H, R[:, :n], c
 
 

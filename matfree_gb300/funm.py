@@ -120,24 +120,55 @@ class MonteCarloFunmSym:
         return length_sq * (self.dense_funm.apply_scalar(lam) * fsq).sum(-1)
 
 
-def slq_values(op, k: int, samples: torch.Tensor, fun: int, param: float, mean_sem=None, workspace=None):
-    """One ``mfg_slq`` call: values (p,) float64 of ||v||^2 e1^T f(T) e1."""
+def two_sweep_applies(op, k: int) -> bool:
+    """Whether ``mfg_slq_ex`` runs the two-sweep step for this operator and k."""
+    return op.basis_dtype == torch.float32 and 2 <= k <= 65
+
+
+def slq_values(op, k: int, samples: torch.Tensor, fun: int, param: float, mean_sem=None,
+               workspace=None, two_sweep=None, check=True):
+    """One ``mfg_slq_ex`` call: values (p,) float64 of ||v||^2 e1^T f(T) e1.
+
+    ``two_sweep`` (default: where it applies) runs the full reorthogonalisation
+    in two reads of the Krylov basis per step.  With ``check`` the call waits
+    for the solve and, if the device reports ``MFG_ERR_RETRY`` (a step whose
+    second projection was too large for the two-sweep form), repeats it with
+    the three-sweep form; callers that keep several solves in flight pass
+    ``check=False`` and call :func:`slq_retry_needed` once the solve is done.
+    """
     p, n = samples.shape
     panel, ld = as_panel(samples, n, op.basis_dtype)
     values = torch.empty((p,), dtype=torch.float64, device=samples.device)
+    if two_sweep is None:
+        two_sweep = two_sweep_applies(op, k)
+    flags = _lib.MFG_SLQ_TWO_SWEEP if two_sweep else 0
     s = op.c_struct()
     lib = _lib.lib()
-    nbytes = lib.mfg_slq_workspace_bytes(ctypes.byref(s), k, p, ld)
+    nbytes = lib.mfg_slq_ex_workspace_bytes(ctypes.byref(s), k, p, ld, flags)
     ws, wsb = (workspace or _WS).get(nbytes, samples.device)
     ms = ctypes.c_void_p(mean_sem.data_ptr()) if mean_sem is not None else ctypes.c_void_p(0)
-    st = lib.mfg_slq(ctypes.byref(s), k, p, ctypes.c_void_p(panel.data_ptr()), ld, fun, param,
-                     ctypes.c_void_p(values.data_ptr()), ms, None, None, ws, wsb, stream_ptr())
+    st = lib.mfg_slq_ex(ctypes.byref(s), k, p, ctypes.c_void_p(panel.data_ptr()), ld, fun, param,
+                        ctypes.c_void_p(values.data_ptr()), ms, None, None, flags, ws, wsb,
+                        stream_ptr())
     err = getattr(op, "error", None)
     if err is not None:
         op.error = None
         raise err
-    _lib.check(st, "mfg_slq")
+    _lib.check(st, "mfg_slq_ex")
+    if two_sweep and check and slq_retry_needed(workspace or _WS):
+        return slq_values(op, k, samples, fun, param, mean_sem, workspace, two_sweep=False)
     return values
+
+
+def slq_retry_needed(workspace) -> bool:
+    """Wait for the last solve on ``workspace``; True if it must be repeated
+    without the two-sweep form (device status ``MFG_ERR_RETRY``)."""
+    buf = workspace.buf
+    st = _lib.lib().mfg_workspace_status(ctypes.c_void_p(buf.data_ptr()), stream_ptr())
+    if st == _lib.MFG_ERR_RETRY:
+        return True
+    _lib.check(st, "mfg_slq_ex (device status)")
+    return False
 
 
 def tridiag_eigh_first(H: torch.Tensor):
