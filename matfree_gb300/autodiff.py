@@ -27,7 +27,7 @@ import torch
 
 from . import _lib
 from ._panel import Workspace, as_panel, padded_ld, require_cuda, stream_ptr
-from .decomp import _tridiag_from_hessenberg, run_hessenberg
+from .decomp import _tridiag_from_hessenberg, run_hessenberg, two_sweep_applies
 from .operators import DenseOperator, RBFKernelOperator
 
 _WS = Workspace()
@@ -130,13 +130,23 @@ def _forward_panels(op, k, panel, ld):
     c = torch.zeros((p,), dtype=torch.float64, device=panel.device)
     s = op.c_struct()
     lib = _lib.lib()
-    nbytes = lib.mfg_slq_workspace_bytes(ctypes.byref(s), k, p, ld)
-    ws, wsb = _WS.get(nbytes, panel.device)
-    st = lib.mfg_hessenberg(ctypes.byref(s), k, p, ctypes.c_void_p(panel.data_ptr()), ld, 1,
-                            ctypes.c_void_p(Q.data_ptr()), ctypes.c_void_p(H.data_ptr()),
-                            ctypes.c_void_p(R.data_ptr()), ctypes.c_void_p(c.data_ptr()), ws, wsb,
-                            stream_ptr())
-    _lib.check(st, "mfg_hessenberg")
+    # full reorthogonalisation in two reads of the basis per step where it
+    # applies, repeated in the three-read form if the device asks for it
+    for mode in ((3, 1) if two_sweep_applies(op, k) else (1,)):
+        flags = _lib.MFG_SLQ_TWO_SWEEP if mode == 3 else 0
+        nbytes = lib.mfg_slq_ex_workspace_bytes(ctypes.byref(s), k, p, ld, flags)
+        ws, wsb = _WS.get(nbytes, panel.device)
+        st = lib.mfg_hessenberg(ctypes.byref(s), k, p, ctypes.c_void_p(panel.data_ptr()), ld, mode,
+                                ctypes.c_void_p(Q.data_ptr()), ctypes.c_void_p(H.data_ptr()),
+                                ctypes.c_void_p(R.data_ptr()), ctypes.c_void_p(c.data_ptr()), ws,
+                                wsb, stream_ptr())
+        _lib.check(st, "mfg_hessenberg")
+        if mode == 1:
+            break
+        dst = lib.mfg_workspace_status(ws, stream_ptr())
+        if dst != _lib.MFG_ERR_RETRY:
+            _lib.check(dst, "mfg_hessenberg (device status)")
+            break
     return Q, H, R, c
 
 

@@ -20,7 +20,7 @@ import torch
 
 from . import _lib
 from ._panel import Workspace, as_panel, require_cuda, stream_ptr
-from .decomp import _flat_operator, _TridiagSymFull, run_hessenberg
+from .decomp import _flat_operator, _TridiagSymFull, run_hessenberg, two_sweep_applies
 from .operators import Operator, as_operator
 from .tree import ravel_pytree
 
@@ -118,11 +118,6 @@ class MonteCarloFunmSym:
         lam, fsq = tridiag_eigh_first(H)
         length_sq = 1.0 / (c * c)
         return length_sq * (self.dense_funm.apply_scalar(lam) * fsq).sum(-1)
-
-
-def two_sweep_applies(op, k: int) -> bool:
-    """Whether ``mfg_slq_ex`` runs the two-sweep step for this operator and k."""
-    return op.basis_dtype == torch.float32 and 2 <= k <= 65
 
 
 def slq_values(op, k: int, samples: torch.Tensor, fun: int, param: float, mean_sem=None,

@@ -78,9 +78,14 @@ def footprint_bytes(n: int, k: int, p: int, precision: str) -> int:
     s.precision = _lib.PRECISIONS[precision]
     s.n, s.lda, s.a = n, ld, 4096
     s.a_lo = 4096 if precision == "bf16x3" else None
-    ws = _lib.lib().mfg_slq_workspace_bytes(ctypes.byref(s), k, p, ld)
+    ws = _lib.lib().mfg_slq_ex_workspace_bytes(ctypes.byref(s), k, p, ld, _flags(k, precision))
     es = 8 if precision == "fp64" else 4
     return int(op_bytes + ws + p * ld * es + n * 3 * 4 + 4096)
+
+
+def _flags(k: int, precision: str) -> int:
+    """Two reads of the Krylov basis per step where that form applies."""
+    return _lib.MFG_SLQ_TWO_SWEEP if precision != "fp64" and 2 <= k <= 65 else 0
 
 
 @dataclass
@@ -101,7 +106,7 @@ class SLQServer:
         self.slots = [_Slot(torch.cuda.Stream(device=self.device)) for _ in range(slots)]
         self.used = 0.0
 
-    def _launch(self, slot: _Slot, req: Request):
+    def _launch(self, slot: _Slot, req: Request, flags=None):
         lib = _lib.lib()
         n = req.x.shape[0]
         ld = padded_ld(n)
@@ -120,18 +125,21 @@ class SLQServer:
             values = torch.empty((req.p,), dtype=torch.float64, device=self.device)
             ms = torch.empty((2,), dtype=torch.float64, device=self.device)
             s = op.c_struct()
-            nbytes = lib.mfg_slq_workspace_bytes(ctypes.byref(s), req.k, req.p, ld)
+            if flags is None:
+                flags = _flags(req.k, self.precision)
+            nbytes = lib.mfg_slq_ex_workspace_bytes(ctypes.byref(s), req.k, req.p, ld, flags)
             ws, wsb = slot.workspace.get(nbytes, self.device)
-            st = lib.mfg_slq(ctypes.byref(s), req.k, req.p, ctypes.c_void_p(probes.data_ptr()), ld, fun, param,
-                             ctypes.c_void_p(values.data_ptr()), ctypes.c_void_p(ms.data_ptr()), None, None,
-                             ws, wsb, ctypes.c_void_p(slot.stream.cuda_stream))
-            _lib.check(st, "mfg_slq")
+            st = lib.mfg_slq_ex(ctypes.byref(s), req.k, req.p, ctypes.c_void_p(probes.data_ptr()), ld, fun,
+                                param, ctypes.c_void_p(values.data_ptr()), ctypes.c_void_p(ms.data_ptr()),
+                                None, None, flags, ws, wsb, ctypes.c_void_p(slot.stream.cuda_stream))
+            _lib.check(st, "mfg_slq_ex")
             out = torch.empty((2,), dtype=torch.float64, pin_memory=True)
             out.copy_(ms, non_blocking=True)
             done = torch.cuda.Event()
             done.record(slot.stream)
         # keep every buffer of the solve alive until its completion event fires
-        return {"done": done, "out": out, "keep": (xh, xd, op, probes, values, ms)}
+        return {"done": done, "out": out, "keep": (xh, xd, op, probes, values, ms), "flags": flags,
+                "ws": ws}
 
     def run(self, requests, *, realtime: bool = True):
         """Serve the requests in arrival order; returns (results, stats)."""
@@ -142,6 +150,11 @@ class SLQServer:
         while pending or inflight:
             now = time.perf_counter() - t0
             for idx, (slot, req, st, fp, t_start) in list(inflight.items()):
+                if st["done"].query() and st["flags"] and _lib.lib().mfg_workspace_status(
+                        st["ws"], ctypes.c_void_p(slot.stream.cuda_stream)) == _lib.MFG_ERR_RETRY:
+                    # the two-sweep step asked for the three-read form: run it again
+                    inflight[idx] = (slot, req, self._launch(slot, req, flags=0), fp, t_start)
+                    continue
                 if st["done"].query():
                     t_end = time.perf_counter() - t0
                     mean, sem = (float(v) for v in st["out"])
