@@ -252,25 +252,36 @@ dense_tcgen05_kernel(const __grid_constant__ CUtensorMap map_ahi,
     const int quarter = warp & 3;
     const int row = quarter * 32 + lane;
     const int m = m0 + row;
+    // The shift term's probe values (shift * V[b][m]) are loaded one group of
+    // 16 probes ahead of the accumulator reads, the first group while the
+    // main loop runs, so their latency stays off the epilogue's path.
+    float sv[16], svn[16];
+    auto load_shift = [&](int c, float(&dst)[16]) {
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        const int b = b0 + c + j;
+        dst[j] = (shift != 0.f && m < n && b < p) ? __ldg(Vf + (int64_t)b * ldvf + m) : 0.f;
+      }
+    };
+    load_shift(0, sv);
     // warp-uniform decision: tcgen05.ld is executed by all 32 lanes or none
     // the epilogue sleeps through the main loop
     const bool ok = __all_sync(0xffffffffu, mbar_wait<true>(&sh->tmem_full, 0, abort_flag, status));
     tc_fence_after();
     if (ok) {
       for (int c = 0; c < BN; c += 16) {
+        if (c + 16 < BN) load_shift(c + 16, svn);
         float v[16];
         tmem_ld16(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)c, v);
         if (m < n) {
 #pragma unroll
           for (int j = 0; j < 16; ++j) {
             const int b = b0 + c + j;
-            if (b < p) {
-              float out = v[j];
-              if (shift != 0.f) out = fmaf(shift, __ldg(Vf + (int64_t)b * ldvf + m), out);
-              W[(int64_t)b * ldw + m] = out;
-            }
+            if (b < p) W[(int64_t)b * ldw + m] = fmaf(shift, sv[j], v[j]);
           }
         }
+#pragma unroll
+        for (int j = 0; j < 16; ++j) sv[j] = svn[j];
       }
     }
   }
@@ -466,23 +477,34 @@ dense_tcgen05_pair_kernel(const __grid_constant__ CUtensorMap map_ahi,
     // epilogue: warps 2..5 -> TMEM lane quarters 2, 3, 0, 1 of this CTA's rows
     const int quarter = warp & 3;
     const int m = m0 + quarter * 32 + lane;
+    // The shift term's probe values (shift * V[b][m]) are loaded one group of
+    // 16 probes ahead of the accumulator reads, the first group while the
+    // main loop runs, so their latency stays off the epilogue's path.
+    float sv[16], svn[16];
+    auto load_shift = [&](int c, float(&dst)[16]) {
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        const int b = b0 + c + j;
+        dst[j] = (shift != 0.f && m < n && b < p) ? __ldg(Vf + (int64_t)b * ldvf + m) : 0.f;
+      }
+    };
+    load_shift(0, sv);
     const bool ok = __all_sync(0xffffffffu, mbar_wait<true>(&sh->tmem_full, 0, abort_flag, status));
     tc_fence_after();
     if (ok) {
       for (int c = 0; c < BN; c += 16) {
+        if (c + 16 < BN) load_shift(c + 16, svn);
         float v[16];
         tmem_ld16(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)c, v);
         if (m < n) {
 #pragma unroll
           for (int j = 0; j < 16; ++j) {
             const int b = b0 + c + j;
-            if (b < p) {
-              float out = v[j];
-              if (shift != 0.f) out = fmaf(shift, __ldg(Vf + (int64_t)b * ldvf + m), out);
-              W[(int64_t)b * ldw + m] = out;
-            }
+            if (b < p) W[(int64_t)b * ldw + m] = fmaf(shift, sv[j], v[j]);
           }
         }
+#pragma unroll
+        for (int j = 0; j < 16; ++j) sv[j] = svn[j];
       }
     }
   }
