@@ -369,8 +369,8 @@ TRAFFIC = {("rbf16k", "bf16x3", "operator apply"): 1.107433e9 + 3.27936e6}
 
 
 def _two_sweep(args, prob):
-    """Whether the solves ran the two-sweep step (float bases, 2 <= k <= 65)."""
-    return args.precision != "fp64" and 2 <= prob["k"] <= 65
+    """Whether the solves ran the two-sweep step (float bases, 2 <= k <= 129)."""
+    return args.precision != "fp64" and 2 <= prob["k"] <= 129
 
 
 def roofline(prof, peaks, steps, config=None, precision=None):

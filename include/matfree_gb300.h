@@ -133,7 +133,7 @@ MFG_API int mfg_operator_apply(const mfg_operator *op, const void *V, void *W, i
  * vectors), 2 = three-term Lanczos of tridiag_sym(reortho="none")
  * (decomp.py:215-291: H holds a_j on the diagonal and b_j below it),
  * 3 = "full" in two basis reads per step (see MFG_SLQ_TWO_SWEEP; falls back
- * to 1 outside float bases with 2 <= k <= 65; workspace from
+ * to 1 outside float bases with 2 <= k <= 129; workspace from
  * mfg_slq_ex_workspace_bytes(..., MFG_SLQ_TWO_SWEEP); check
  * mfg_workspace_status for MFG_ERR_RETRY). */
 MFG_API int mfg_hessenberg(const mfg_operator *op, int64_t k, int64_t p, const void *V,
@@ -188,7 +188,7 @@ MFG_API int mfg_slq(const mfg_operator *op, int64_t k, int64_t p, const void *pr
  * projection of step j-1 is done together with the first projection of step
  * j, and A q_j is recovered from A applied to the not yet reorthogonalised
  * vector through the Arnoldi relation).  H, and so values, equal mfg_slq's to
- * rounding.  Applies to float bases with 2 <= k <= 65 (otherwise the call
+ * rounding.  Applies to float bases with 2 <= k <= 129 (otherwise the call
  * runs mfg_slq).  When a step's second projection exceeds 0.1 of the vector
  * (a vector left largely inside the basis by one projection, near an
  * invariant subspace) the rounding of the recovered product is no longer

@@ -98,10 +98,9 @@ static int elem_size_for(const mfg_operator *op) {
   return op->precision == MFG_PREC_FP64 ? 8 : 4;
 }
 
-// The two-sweep step covers float bases of up to 65 vectors (its two-vector
-// passes keep both vectors' per-thread sums in registers).
+// The two-sweep step covers float bases of 2 <= k <= kTwoSweepMaxK vectors.
 static bool two_sweep_applies(const mfg_operator *op, int64_t k) {
-  return op->precision != MFG_PREC_FP64 && k >= 2 && k <= kTwoSweepMaxCols + 1;
+  return op->precision != MFG_PREC_FP64 && k >= 2 && k <= kTwoSweepMaxK;
 }
 
 static bool uses_bf16(const mfg_operator *op) {
@@ -293,14 +292,25 @@ static int run_two_sweep(const mfg_operator *op, int64_t k, int64_t p, int64_t l
     for (int64_t j = 1; j < k; ++j) {
       const int nc = (int)j;
       MFG_LAUNCH(MFG_PROF_APPLY, ab, af, apply_op<T>(op, Vt, ld, Wb, ld, p, hi, lo, ld, panel, status, s));
-      // [Q^T qt | Q^T w | qt . w] from one read of the basis
-      MFG_LAUNCH(MFG_PROF_PROJ, (nc + 2.0) * vecb, 4.0 * nc * vecb / sizeof(T),
-                 launch_proj2<T>(Q, qb, ld, nc, Wb, Vt, ld, n, p, partials, counters, X2, xs,
-                                 koff, status, s));
-      // q_j (unnormalised) = qt - Q Q^T qt into row j, w <- w - Q Q^T w
-      MFG_LAUNCH(MFG_PROF_SUBPROJ, (nc + 4.0) * vecb, 4.0 * nc * vecb / sizeof(T),
-                 launch_sub2<T>(Q, qb, ld, nc, X2, xs, koff, Wb, Vt, ld, Q + j * ld, qb, n, p,
-                                partials, counters, dots, status, s));
+      // [Q^T qt | Q^T w | qt . w] from one read of the basis, in column blocks
+      // of at most kTwoSweepPassCols vectors (the later blocks' qt . w goes to
+      // a scratch slot: it is the first block's value again)
+      for (int c0 = 0; c0 < nc; c0 += kTwoSweepPassCols) {
+        const int cn = nc - c0 < kTwoSweepPassCols ? nc - c0 : kTwoSweepPassCols;
+        MFG_LAUNCH(MFG_PROF_PROJ, (cn + 2.0) * vecb, 4.0 * cn * vecb / sizeof(T),
+                   launch_proj2<T>(Q, qb, ld, c0, cn, Wb, Vt, ld, n, p, partials, counters,
+                                   X2 + c0, xs, koff, c0 > 0 ? dots : nullptr, 3, status, s));
+      }
+      // q_j (unnormalised) = qt - Q Q^T qt into row j, w <- w - Q Q^T w; a
+      // later column block continues from the first block's results
+      for (int c0 = 0; c0 < nc; c0 += kTwoSweepPassCols) {
+        const int cn = nc - c0 < kTwoSweepPassCols ? nc - c0 : kTwoSweepPassCols;
+        const T *bin = c0 == 0 ? Vt : Q + j * ld;
+        const int64_t bstr = c0 == 0 ? ld : qb;
+        MFG_LAUNCH(MFG_PROF_SUBPROJ, (cn + 4.0) * vecb, 4.0 * cn * vecb / sizeof(T),
+                   launch_sub2<T>(Q, qb, ld, c0, cn, X2 + c0, xs, koff, Wb, ld, bin, bstr,
+                                  Q + j * ld, qb, n, p, partials, counters, dots, status, s));
+      }
       MFG_LAUNCH(MFG_PROF_OTHER, 8.0 * p * (3.0 * k + 2.0 * j), 2.0 * p * j * j,
                  launch_twosweep_coef((int)j, (int)k, p, X2, koff, dots, H, Hh, nu, cf, status, s));
       const bool more = j + 1 < k;

@@ -33,18 +33,21 @@ int launch_scale(const T *Win, int64_t w_bstride, int64_t n, int64_t p, const do
                  int64_t out_bstride, __nv_bfloat16 *hi, __nv_bfloat16 *lo, int64_t bf_bstride,
                  cudaStream_t s);
 int launch_inv(const double *x, double *y, int64_t p, cudaStream_t s);
-// two-sweep Arnoldi step (lanczos_kernels.cu; float bases, ncols <= kTwoSweepMaxCols)
-constexpr int kTwoSweepMaxCols = 64;
+// two-sweep Arnoldi step (lanczos_kernels.cu; float bases).  One two-vector
+// pass covers at most kTwoSweepPassCols basis vectors (both vectors' sums stay
+// in registers); steps with more run it on column blocks.  k <= kTwoSweepMaxK.
+constexpr int kTwoSweepPassCols = 64;
+constexpr int kTwoSweepMaxK = 129;
 template <typename T>
-int launch_proj2(const T *Q, int64_t q_bstride, int64_t q_istride, int ncols, const T *Wa,
-                 const T *Wb, int64_t w_bstride, int64_t n, int64_t p, double *partials,
-                 unsigned *counters, double *out, int64_t out_bstride, int64_t koff, int *status,
-                 cudaStream_t s);
+int launch_proj2(const T *Q, int64_t q_bstride, int64_t q_istride, int coff, int ncols,
+                 const T *Wa, const T *Wb, int64_t w_bstride, int64_t n, int64_t p,
+                 double *partials, unsigned *counters, double *out, int64_t out_bstride,
+                 int64_t koff, double *cross, int64_t cross_bstride, int *status, cudaStream_t s);
 template <typename T>
-int launch_sub2(const T *Q, int64_t q_bstride, int64_t q_istride, int ncols, const double *coef,
-                int64_t c_bstride, int64_t koff, T *Wa, const T *Wb, int64_t w_bstride, T *Wo,
-                int64_t wo_bstride, int64_t n, int64_t p, double *partials, unsigned *counters,
-                double *dots, int *status, cudaStream_t s);
+int launch_sub2(const T *Q, int64_t q_bstride, int64_t q_istride, int coff, int ncols,
+                const double *coef, int64_t c_bstride, int64_t koff, T *Wa, int64_t wa_bstride,
+                const T *Wb, int64_t wb_bstride, T *Wo, int64_t wo_bstride, int64_t n, int64_t p,
+                double *partials, unsigned *counters, double *dots, int *status, cudaStream_t s);
 int launch_twosweep_coef(int j, int k, int64_t p, const double *X2, int64_t koff,
                          const double *dots, double *H, double *Hh, double *nu, double *cf,
                          int *status, cudaStream_t s);

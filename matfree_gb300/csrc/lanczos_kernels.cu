@@ -539,7 +539,8 @@ stream_sweep_kernel(const __grid_constant__ CUtensorMap qmap, const T *__restric
                     int64_t q_bstride, int64_t q_istride, int ncols,
                     const double *__restrict__ coef, int64_t c_bstride, int64_t c_istride,
                     T *Wv, int64_t w_bstride, const T *Wv2, int64_t w2_bstride, T *Wo2,
-                    int64_t wo2_bstride, int64_t koff, int64_t n, int64_t p, int nbuf, int pstride,
+                    int64_t wo2_bstride, int64_t koff, int coff, int64_t n, int64_t p, int nbuf,
+                    int pstride,
                     double *__restrict__ partials, unsigned *__restrict__ counters,
                     double *__restrict__ out, int64_t out_bstride, int64_t out_istride,
                     double *__restrict__ out2, int64_t out2_bstride, int *__restrict__ status) {
@@ -627,7 +628,7 @@ stream_sweep_kernel(const __grid_constant__ CUtensorMap qmap, const T *__restric
       T *dst = bufs + u * bstr;
       for (int c = lane; c < ncopies; c += 32) {
         if (c < full) {
-          const int x = (int)r0, y = (int)(b * kcols + c * kSPGroup);
+          const int x = (int)r0, y = (int)(b * kcols + coff + c * kSPGroup);
           asm volatile(
               "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes "
               "[%0], [%1, {%3, %4}], [%2];" ::"r"(smem_addr(dst + (size_t)c * kSPGroup * kSR)),
@@ -640,7 +641,7 @@ stream_sweep_kernel(const __grid_constant__ CUtensorMap qmap, const T *__restric
           const int vec = c - (ncopies - kNV);  // 0: w, 1: second vector, < 0: basis
           const T *src = vec == 0   ? Wv + b * w_bstride + r0
                          : vec == 1 ? Wv2 + b * w2_bstride + r0
-                                    : Q + b * q_bstride + (int64_t)i * q_istride + r0;
+                                    : Q + b * q_bstride + (int64_t)(coff + i) * q_istride + r0;
           T *d = dst + (size_t)(vec >= 0 ? cpad + vec : i) * kSR;
           asm volatile(
               "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
@@ -895,7 +896,10 @@ stream_sweep_kernel(const __grid_constant__ CUtensorMap qmap, const T *__restric
             } else if constexpr (kMode == kStreamProj2) {
               constexpr int kHalf = kSPGroup * MAXG;
               if (v == 2 * kHalf) {
-                out[b * out_bstride + 2 * koff] = h[o];
+                if (out2)
+                  out2[b * out2_bstride] = h[o];
+                else
+                  out[b * out_bstride + 2 * koff] = h[o];
               } else {
                 const int half = v / kHalf, i = v - half * kHalf;
                 if (i < ncols) out[b * out_bstride + half * koff + i] = h[o];
@@ -962,6 +966,7 @@ struct StreamArgs {
   int64_t w2_bstride = 0;
   void *Wo2 = nullptr;
   int64_t wo2_bstride = 0, koff = 0;
+  int coff = 0;  // first basis vector of the pass (the vectors are coff .. coff + ncols - 1)
 };
 
 template <typename T, int MAXG, bool kHold, int kMode>
@@ -1014,7 +1019,7 @@ static int launch_stream_sweep_t(const StreamArgs &a, cudaStream_t s) {
   kern<<<(unsigned)G, kSThreads + 32, smem, s>>>(
       qmap, static_cast<const T *>(a.Q), a.q_bstride, a.q_istride, a.ncols, a.coef, a.c_bstride,
       a.c_istride, static_cast<T *>(a.Wv), a.w_bstride, static_cast<const T *>(a.Wv2),
-      a.w2_bstride, static_cast<T *>(a.Wo2), a.wo2_bstride, a.koff, a.n, a.p, nbuf, pstride,
+      a.w2_bstride, static_cast<T *>(a.Wo2), a.wo2_bstride, a.koff, a.coff, a.n, a.p, nbuf, pstride,
       a.partials, a.counters, a.out, a.out_bstride, a.out_istride, a.out2, a.out2_bstride,
       a.status);
   return MFG_LAUNCH_STATUS();
@@ -1028,7 +1033,7 @@ static int launch_stream_sweep(const StreamArgs &a, cudaStream_t s) {
     if constexpr (sizeof(T) != 4) {
       return MFG_ERR_UNSUPPORTED;
     } else {
-      if (a.ncols < 1 || a.ncols > kTwoSweepMaxCols) return MFG_ERR_UNSUPPORTED;
+      if (a.ncols < 1 || a.ncols > kTwoSweepPassCols) return MFG_ERR_UNSUPPORTED;
       if (a.ncols <= 8) return launch_stream_sweep_t<T, 1, false, kMode>(a, s);
       if (a.ncols <= 32) return launch_stream_sweep_t<T, 4, false, kMode>(a, s);
       return launch_stream_sweep_t<T, 8, false, kMode>(a, s);
@@ -1354,37 +1359,43 @@ int launch_cg_direction(T *P, const T *R, int64_t ld, int64_t n, int64_t p, cons
 // three-sweep form.
 // ---------------------------------------------------------------------------
 
-// a = w (per probe rows of w_bstride), b = qt: out[b] = [Q^T qt (k) | Q^T w (k) | qt . w]
+// Basis vectors coff .. coff + ncols - 1 against a = w (per probe rows of
+// w_bstride) and b = qt: out[b] = [Q^T qt (ncols) | at koff: Q^T w (ncols) | at
+// 2 koff: qt . w], the last into cross[b * cross_bstride] instead when cross
+// is given.
 template <typename T>
-int launch_proj2(const T *Q, int64_t q_bstride, int64_t q_istride, int ncols, const T *Wa,
-                 const T *Wb, int64_t w_bstride, int64_t n, int64_t p, double *partials,
-                 unsigned *counters, double *out, int64_t out_bstride, int64_t koff, int *status,
-                 cudaStream_t s) {
+int launch_proj2(const T *Q, int64_t q_bstride, int64_t q_istride, int coff, int ncols,
+                 const T *Wa, const T *Wb, int64_t w_bstride, int64_t n, int64_t p,
+                 double *partials, unsigned *counters, double *out, int64_t out_bstride,
+                 int64_t koff, double *cross, int64_t cross_bstride, int *status, cudaStream_t s) {
   if (ncols <= 0 || p <= 0) return MFG_OK;
   StreamArgs a{Q,        q_bstride,   q_istride, ncols,   nullptr,  0,       0,
                const_cast<T *>(Wa), w_bstride, n,       p,        partials, counters,
-               out,      out_bstride, 1,         nullptr, 0,        status};
+               out,      out_bstride, 1,         cross,   cross_bstride, status};
   a.Wv2 = Wb;
   a.w2_bstride = w_bstride;
   a.koff = koff;
+  a.coff = coff;
   return launch_stream_sweep<T, kStreamProj2>(a, s);
 }
 
-// Wa <- Wa - Q g (coef + koff), Wo <- Wb - Q h (coef); dots[b] = (||Wo||^2, ||Wa||^2, Wo . Wa)
+// Basis vectors coff .. coff + ncols - 1: Wa <- Wa - Q g (coef + koff),
+// Wo <- Wb - Q h (coef); dots[b] = (||Wo||^2, ||Wa||^2, Wo . Wa).  Wo may be Wb.
 template <typename T>
-int launch_sub2(const T *Q, int64_t q_bstride, int64_t q_istride, int ncols, const double *coef,
-                int64_t c_bstride, int64_t koff, T *Wa, const T *Wb, int64_t w_bstride, T *Wo,
-                int64_t wo_bstride, int64_t n, int64_t p, double *partials, unsigned *counters,
-                double *dots, int *status, cudaStream_t s) {
+int launch_sub2(const T *Q, int64_t q_bstride, int64_t q_istride, int coff, int ncols,
+                const double *coef, int64_t c_bstride, int64_t koff, T *Wa, int64_t wa_bstride,
+                const T *Wb, int64_t wb_bstride, T *Wo, int64_t wo_bstride, int64_t n, int64_t p,
+                double *partials, unsigned *counters, double *dots, int *status, cudaStream_t s) {
   if (ncols <= 0 || p <= 0) return MFG_OK;
-  StreamArgs a{Q,  q_bstride, q_istride, ncols,   coef,     c_bstride, 1,
-               Wa, w_bstride, n,         p,       partials, counters,  dots,
-               3,  1,         nullptr,   0,       status};
+  StreamArgs a{Q,  q_bstride,  q_istride, ncols,   coef,     c_bstride, 1,
+               Wa, wa_bstride, n,         p,       partials, counters,  dots,
+               3,  1,          nullptr,   0,       status};
   a.Wv2 = Wb;
-  a.w2_bstride = w_bstride;
+  a.w2_bstride = wb_bstride;
   a.Wo2 = Wo;
   a.wo2_bstride = wo_bstride;
   a.koff = koff;
+  a.coff = coff;
   return launch_stream_sweep<T, kStreamSub2>(a, s);
 }
 
@@ -1400,6 +1411,9 @@ __global__ void twosweep_coef_kernel(int j, int k, int64_t p, const double *__re
                                      double *__restrict__ H, double *__restrict__ Hh,
                                      double *__restrict__ nu, double *__restrict__ cf,
                                      int *__restrict__ status) {
+  // j <= kTwoSweepMaxK - 1 = 128: columns in 4 blocks of 32 lanes, rows
+  // (0 .. j) in 5 blocks
+  constexpr int kCB = 4, kRB = 5;
   const int lane = threadIdx.x & 31;
   const int64_t b = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (b >= p) return;  // warp-uniform
@@ -1407,63 +1421,87 @@ __global__ void twosweep_coef_kernel(int j, int k, int64_t p, const double *__re
   double *Hb = H + b * (int64_t)k * k;
   double *Hhb = Hh + b * (int64_t)(k + 1) * k;  // column-major: column l at Hhb + l (k + 1)
   const int64_t ld = k + 1;
-  // every input first, in one round of independent loads; lane owns rows
-  // lane, lane + 32 and lane + 64 (j <= 64)
+  // every input first, in one round of independent loads
   const double nb = dots[b * 3], nz = dots[b * 3 + 1], bz = dots[b * 3 + 2];
   const double c = x[2 * koff], nuj = nu[b];
-  const bool r0 = lane < j, r1 = lane + 32 < j;
-  const double hq0 = r0 ? x[lane] : 0.0, hq1 = r1 ? x[lane + 32] : 0.0;
-  const double g0 = r0 ? x[koff + lane] : 0.0, g1 = r1 ? x[koff + lane + 32] : 0.0;
-  const double hp0 = r0 ? Hb[(int64_t)lane * k + (j - 1)] : 0.0;
-  const double hp1 = r1 ? Hb[(int64_t)(lane + 32) * k + (j - 1)] : 0.0;
-  const double hh = warp_sum(fma(hq0, hq0, hq1 * hq1));
-  const double hg = warp_sum(fma(hq0, g0, hq1 * g1));
+  double hq[kCB], g[kCB], hp[kCB];
+#pragma unroll
+  for (int cb = 0; cb < kCB; ++cb) {
+    const int l = lane + 32 * cb;
+    const bool ok = l < j;
+    hq[cb] = ok ? x[l] : 0.0;
+    g[cb] = ok ? x[koff + l] : 0.0;
+    hp[cb] = ok ? Hb[(int64_t)l * k + (j - 1)] : 0.0;
+  }
+  double hh = 0.0, hg = 0.0;
+#pragma unroll
+  for (int cb = 0; cb < kCB; ++cb) {
+    hh = fma(hq[cb], hq[cb], hh);
+    hg = fma(hq[cb], g[cb], hg);
+  }
+  hh = warp_sum(hh);
+  hg = warp_sum(hg);
   const double rho = sqrt(nb);   // ||w''_{j-1}|| / nu_j
   const double beta = nuj * rho;
   // column j-1 of Hh (the reference's h_{j-1} plus the second projection,
-  // beta below it), kept in registers for the product below
-  const double cj0 = r0 ? hp0 + nuj * hq0 : (lane == j ? beta : 0.0);
-  const double cj1 = r1 ? hp1 + nuj * hq1 : (lane + 32 == j ? beta : 0.0);
-  const double cj2 = lane + 64 == j ? beta : 0.0;
+  // beta below it) for the rows lane + 32 r, kept in registers
+  double cj[kRB];
+#pragma unroll
+  for (int r = 0; r < kRB; ++r) {
+    const int i = lane + 32 * r;
+    const double up = r < kCB ? hp[r < kCB ? r : 0] + nuj * hq[r < kCB ? r : 0] : 0.0;
+    cj[r] = i < j ? up : (i == j ? beta : 0.0);
+  }
   double *col = Hhb + (int64_t)(j - 1) * ld;
-  if (lane <= j) col[lane] = cj0;
-  if (lane + 32 <= j) col[lane + 32] = cj1;
-  if (lane + 64 <= j) col[lane + 64] = cj2;
+#pragma unroll
+  for (int r = 0; r < kRB; ++r)
+    if (lane + 32 * r <= j) col[lane + 32 * r] = cj[r];
   if (lane == 0) Hb[(int64_t)j * k + (j - 1)] = beta;
   const double qw = (c - hg) / rho;  // q_j . A qt_j
   if (j < k) {
     // m = Hh[0:j+1, 0:j] hq: all lanes walk the same columns (hq_l broadcast
     // by shuffle), eight columns of loads in flight; entries below the
     // subdiagonal (never written) are masked
-    double m0 = 0.0, m1 = 0.0, m2 = 0.0;
+    double m[kRB];
+#pragma unroll
+    for (int r = 0; r < kRB; ++r) m[r] = 0.0;
     for (int l0 = 0; l0 < j - 1; l0 += 8) {
-      double a0[8], a1[8], a2[8];
+      double a[8][kRB];
 #pragma unroll
       for (int t = 0; t < 8; ++t) {
         const int l = l0 + t;
         const double *cl = Hhb + (int64_t)l * ld;
-        const bool ok = l < j - 1;
-        a0[t] = ok && lane <= l + 1 ? cl[lane] : 0.0;
-        a1[t] = ok && lane + 32 <= l + 1 ? cl[lane + 32] : 0.0;
-        a2[t] = ok && lane + 64 <= l + 1 ? cl[lane + 64] : 0.0;
+#pragma unroll
+        for (int r = 0; r < kRB; ++r) {
+          const int i = lane + 32 * r;
+          a[t][r] = (l < j - 1 && i <= l + 1) ? cl[i] : 0.0;
+        }
       }
 #pragma unroll
       for (int t = 0; t < 8; ++t) {
         const int l = l0 + t;
-        const double hv = __shfl_sync(0xffffffffu, l < 32 ? hq0 : hq1, l & 31);
-        m0 = fma(a0[t], hv, m0);
-        m1 = fma(a1[t], hv, m1);
-        m2 = fma(a2[t], hv, m2);
+        const double src = l < 32 ? hq[0] : (l < 64 ? hq[1] : (l < 96 ? hq[2] : hq[3]));
+        const double hv = __shfl_sync(0xffffffffu, src, l & 31);
+#pragma unroll
+        for (int r = 0; r < kRB; ++r) m[r] = fma(a[t][r], hv, m[r]);
       }
     }
-    const double hv = __shfl_sync(0xffffffffu, j - 1 < 32 ? hq0 : hq1, (j - 1) & 31);
-    m0 = fma(cj0, hv, m0);
-    m1 = fma(cj1, hv, m1);
-    m2 = fma(cj2, hv, m2);
+    {
+      const int l = j - 1;
+      const double src = l < 32 ? hq[0] : (l < 64 ? hq[1] : (l < 96 ? hq[2] : hq[3]));
+      const double hv = __shfl_sync(0xffffffffu, src, l & 31);
+#pragma unroll
+      for (int r = 0; r < kRB; ++r) m[r] = fma(cj[r], hv, m[r]);
+    }
     // h_j = (nu [g; qw] - m) / beta into column j of H
-    if (lane <= j) Hb[(int64_t)lane * k + j] = nuj * ((r0 ? g0 : qw) - m0) / beta;
-    if (lane + 32 <= j) Hb[(int64_t)(lane + 32) * k + j] = nuj * ((r1 ? g1 : qw) - m1) / beta;
-    if (lane + 64 <= j) Hb[(int64_t)(lane + 64) * k + j] = nuj * (qw - m2) / beta;
+#pragma unroll
+    for (int r = 0; r < kRB; ++r) {
+      const int i = lane + 32 * r;
+      if (i <= j) {
+        const double top = (r < kCB && i < j) ? g[r < kCB ? r : 0] : qw;
+        Hb[(int64_t)i * k + j] = nuj * (top - m[r]) / beta;
+      }
+    }
   }
   if (lane == 0) {
     if (hh > 0.01 * (hh + nb) && status) atomicExch(status, (int)MFG_ERR_RETRY);
@@ -1555,13 +1593,14 @@ int launch_twosweep_finish(T *Qj, int64_t q_bstride, const T *Z, int64_t w_bstri
   return MFG_LAUNCH_STATUS();
 }
 
-template int launch_proj2<float>(const float *, int64_t, int64_t, int, const float *,
+template int launch_proj2<float>(const float *, int64_t, int64_t, int, int, const float *,
                                  const float *, int64_t, int64_t, int64_t, double *, unsigned *,
-                                 double *, int64_t, int64_t, int *, cudaStream_t);
-template int launch_sub2<float>(const float *, int64_t, int64_t, int, const double *, int64_t,
-                                int64_t, float *, const float *, int64_t, float *, int64_t,
-                                int64_t, int64_t, double *, unsigned *, double *, int *,
-                                cudaStream_t);
+                                 double *, int64_t, int64_t, double *, int64_t, int *,
+                                 cudaStream_t);
+template int launch_sub2<float>(const float *, int64_t, int64_t, int, int, const double *,
+                                int64_t, int64_t, float *, int64_t, const float *, int64_t,
+                                float *, int64_t, int64_t, int64_t, double *, unsigned *,
+                                double *, int *, cudaStream_t);
 template int launch_twosweep_finish<float>(float *, int64_t, const float *, int64_t, int64_t,
                                            int64_t, const double *, float *, __nv_bfloat16 *,
                                            __nv_bfloat16 *, int64_t, cudaStream_t);

@@ -45,8 +45,8 @@ _WS = Workspace()
 def two_sweep_applies(op, k: int) -> bool:
     """Whether the two-sweep step (``mfg_slq_ex`` flag MFG_SLQ_TWO_SWEEP,
     ``mfg_hessenberg`` reortho 3) runs for this operator and k: float bases,
-    2 <= k <= 65."""
-    return op.basis_dtype == torch.float32 and 2 <= k <= 65
+    2 <= k <= 129."""
+    return op.basis_dtype == torch.float32 and 2 <= k <= 129
 
 
 def run_hessenberg(op, k: int, V: torch.Tensor, *, reortho: str = "full", workspace=None):

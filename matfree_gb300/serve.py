@@ -85,7 +85,7 @@ def footprint_bytes(n: int, k: int, p: int, precision: str) -> int:
 
 def _flags(k: int, precision: str) -> int:
     """Two reads of the Krylov basis per step where that form applies."""
-    return _lib.MFG_SLQ_TWO_SWEEP if precision != "fp64" and 2 <= k <= 65 else 0
+    return _lib.MFG_SLQ_TWO_SWEEP if precision != "fp64" and 2 <= k <= 129 else 0
 
 
 @dataclass

@@ -30,7 +30,8 @@ def _t(x, dtype=torch.float64):
     return torch.as_tensor(np.asarray(x), dtype=dtype, device="cuda")
 
 
-@pytest.mark.parametrize("n,k,p", [(300, 2, 3), (300, 40, 5), (1000, 64, 4), (700, 65, 3)])
+@pytest.mark.parametrize("n,k,p", [(300, 2, 3), (300, 40, 5), (1000, 64, 4), (700, 65, 3),
+                                   (700, 66, 2), (1500, 100, 3), (900, 129, 2)])
 def test_two_sweep_hessenberg_matches_oracle_and_three_sweep(n, k, p):
     A = problems.dense_spd(n, seed=n + k)
     A32 = A.astype(np.float32).astype(np.float64)
@@ -99,13 +100,13 @@ def test_two_sweep_falls_back_near_an_invariant_subspace():
 
 
 def test_two_sweep_outside_its_range_is_the_three_sweep_form():
-    # k = 66 and float64 bases run the three-read form unchanged
+    # k = 130 and float64 bases run the three-read form unchanged
     n = 300
     A = problems.dense_spd(n, seed=1)
     V = np.random.default_rng(2).standard_normal((2, n))
     op = mf.DenseOperator(_t(A, torch.float32), precision="fp32")
-    _, H2, _, _ = run_hessenberg(op, 66, _t(V, torch.float32), reortho="full-two-sweep")
-    _, H1, _, _ = run_hessenberg(op, 66, _t(V, torch.float32), reortho="full")
+    _, H2, _, _ = run_hessenberg(op, 130, _t(V, torch.float32), reortho="full-two-sweep")
+    _, H1, _, _ = run_hessenberg(op, 130, _t(V, torch.float32), reortho="full")
     assert torch.equal(H2, H1)
     op64 = mf.DenseOperator(_t(A), precision="fp64")
     _, H2, _, _ = run_hessenberg(op64, 20, _t(V), reortho="full-two-sweep")
