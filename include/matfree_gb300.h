@@ -168,6 +168,15 @@ MFG_API int mfg_hessenberg_adjoint(const mfg_operator *op, int64_t k, int64_t p,
  * NULL; scale may be NULL (1).
  * Replaces funm.dense_funm_sym_eigh + the quadform's e1^T f(T) e1
  * (matfree/funm.py:239-241, 322-335) and decomp.py:133-135. */
+/* Eigenvalues (ascending, eigvals p x k) and every eigenvector (eigvecs p
+ * k x k, row-major, column j = eigenvector j) of the symmetric tridiagonal
+ * part of (H + H^T)/2 for p Hessenberg matrices (implicit QL, one warp per
+ * problem); scratch holds p k x k doubles.  The dense eigh that the
+ * derivative of e1^T f(T) e1 uses (matfree/funm.py:322-335 under
+ * autodiff). */
+MFG_API int mfg_tridiag_eigh(int64_t k, int64_t p, const double *H, double *eigvals,
+                             double *eigvecs, double *scratch, void *stream);
+
 MFG_API int mfg_tridiag_quadrature(int64_t k, int64_t p, const double *H, int32_t fun,
                            double param, const double *scale, double *values,
                            double *eigvals, double *first_sq, void *stream);

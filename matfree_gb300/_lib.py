@@ -67,6 +67,7 @@ SIGNATURES = {
     "mfg_slq_ex_workspace_bytes": (c_size_t, [POINTER(MfgOperator), c_int64, c_int64, c_int64, c_int32]),
     "mfg_slq_ex": (c_int, [POINTER(MfgOperator), c_int64, c_int64, c_void_p, c_int64, c_int32, c_double, c_void_p, c_void_p, c_void_p, c_void_p, c_int32, c_void_p, c_size_t, c_void_p]),
     "mfg_workspace_status": (c_int, [c_void_p, c_void_p]),
+    "mfg_tridiag_eigh": (c_int, [c_int64, c_int64, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     "mfg_rbf_build": (c_int, [c_void_p, c_int64, c_int32, c_double, c_double, c_int32, c_void_p, c_void_p, c_int64, c_void_p]),
     "mfg_rbf_build_dlogell": (c_int, [c_void_p, c_int64, c_int32, c_double, c_double, c_int32, c_void_p, c_void_p, c_int64, c_void_p]),
     "mfg_split_bf16": (c_int, [c_void_p, c_int64, c_int64, c_int64, c_void_p, c_void_p, c_int64, c_void_p]),

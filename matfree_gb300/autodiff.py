@@ -27,7 +27,7 @@ import torch
 
 from . import _lib
 from ._panel import Workspace, as_panel, padded_ld, require_cuda, stream_ptr
-from .decomp import _tridiag_from_hessenberg, run_hessenberg, two_sweep_applies
+from .decomp import run_hessenberg, two_sweep_applies
 from .operators import DenseOperator, RBFKernelOperator
 
 _WS = Workspace()
@@ -38,10 +38,10 @@ def quadform_dH(H: torch.Tensor, scale: torch.Tensor, f, fprime) -> tuple[torch.
 
     H: (p, k, k) float64; scale: (p,) float64.  Returns (values (p,), dH (p, k, k)).
     """
-    d, e = _tridiag_from_hessenberg(H)
-    p, k = d.shape
-    T = torch.diag_embed(d) + torch.diag_embed(e, 1) + torch.diag_embed(e, -1)
-    w, S = torch.linalg.eigh(T)
+    from .funm import tridiag_eigh
+
+    p, k = H.shape[0], H.shape[1]
+    w, S = tridiag_eigh(H)  # the eigh of T = tridiagonal part of (H + H^T)/2
     fw = f(w)
     s1 = S[:, 0, :]
     values = scale * (fw * s1 * s1).sum(-1)

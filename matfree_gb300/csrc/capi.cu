@@ -1080,6 +1080,15 @@ int mfg_hessenberg_adjoint(const mfg_operator *op, int64_t k, int64_t p, int64_t
                             dH, (const float *)dr, dc, (float *)Lambda, (float *)dv, L, ws, s);
 }
 
+int mfg_tridiag_eigh(int64_t k, int64_t p, const double *H, double *eigvals, double *eigvecs,
+                     double *scratch, void *stream) {
+  if (k <= 0 || p <= 0 || !H || !eigvals || !eigvecs || !scratch) return MFG_ERR_BAD_ARG;
+  cudaStream_t s = as_stream(stream);
+  MFG_LAUNCH(MFG_PROF_QUAD, 8.0 * p * k * k * 3.0, 6.0 * p * k * k * k,
+             launch_tridiag_eigh_full(k, p, H, eigvals, eigvecs, scratch, nullptr, s));
+  return MFG_OK;
+}
+
 int mfg_tridiag_quadrature(int64_t k, int64_t p, const double *H, int32_t fun, double param,
                            const double *scale, double *values, double *eigvals, double *first_sq,
                            void *stream) {

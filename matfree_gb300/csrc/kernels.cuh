@@ -84,6 +84,8 @@ int launch_adj_lincomb(const T *U, const T *lam, const T *R, const double *scal,
                        int64_t ld, int64_t p, T *out, cudaStream_t s);
 
 // tridiag_quadrature.cu
+int launch_tridiag_eigh_full(int64_t k, int64_t p, const double *H, double *w, double *S,
+                             double *Z, int *status, cudaStream_t s);
 int launch_tridiag_quadrature(int64_t k, int64_t p, const double *H, int32_t fun, double param,
                               const double *scale, double *values, double *eigvals,
                               double *first_sq, int *status, cudaStream_t s);

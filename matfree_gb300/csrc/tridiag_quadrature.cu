@@ -152,6 +152,134 @@ __global__ void tridiag_ql_kernel(int k, int64_t p, const double *__restrict__ H
 #undef Z_
 }
 
+// ------------------------------------------------- full eigenvectors, warp per problem
+//
+// Eigenvalues (ascending) and the full eigenvector matrix of each T, for the
+// derivative of e1^T f(T) e1 (the Daleckii-Krein form needs every
+// eigenvector).  Implicit QL with Wilkinson shifts as above; every lane of
+// the warp runs the same shift chase on the warp's d, e (identical
+// arithmetic, so identical values), and applies each rotation to its own rows
+// of Z (rows lane, lane + 32, ...).  Z (scratch) is row-major k x k; the
+// sorted eigenvectors go to S as columns (S[r][j] = component r of vector j).
+
+__global__ void tridiag_eigh_full_kernel(int k, int64_t p, const double *__restrict__ H,
+                                         double *__restrict__ w_out, double *__restrict__ S,
+                                         double *__restrict__ Z, int *__restrict__ status) {
+  extern __shared__ double smf[];
+  const int lane = threadIdx.x & 31;
+  const int64_t b = blockIdx.x;
+  if (b >= p) return;
+  double *d = smf;
+  double *e = d + k;
+  int *perm = reinterpret_cast<int *>(e + k);
+  const double *Hb = H + (size_t)b * k * k;
+  double *Zb = Z + (size_t)b * k * k;
+  for (int i = lane; i < k; i += 32) {
+    d[i] = Hb[(size_t)i * k + i];
+    e[i] = (i + 1 < k) ? 0.5 * (Hb[(size_t)i * k + i + 1] + Hb[(size_t)(i + 1) * k + i]) : 0.0;
+  }
+  for (int r = lane; r < k; r += 32)
+    for (int c = 0; c < k; ++c) Zb[(size_t)r * k + c] = r == c ? 1.0 : 0.0;
+  __syncwarp();
+  bool ok = true;
+  for (int l = 0; l < k && ok; ++l) {
+    int sweeps = 0;
+    while (true) {
+      int m = l;
+      for (; m < k - 1; ++m) {
+        const double dd = fabs(d[m]) + fabs(d[m + 1]);
+        if (fabs(e[m]) <= DBL_EPSILON * dd) break;
+      }
+      if (m == l) break;
+      if (++sweeps > kMaxSweeps) {
+        ok = false;
+        break;
+      }
+      double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
+      double r = hypot(g, 1.0);
+      g = d[m] - d[l] + e[l] / (g + copysign(r, g));
+      double sn = 1.0, cs = 1.0, shift_acc = 0.0;
+      bool deflated = false;
+      for (int i = m - 1; i >= l; --i) {
+        const double f = sn * e[i];
+        const double bb = cs * e[i];
+        const double rr = fma(f, f, g * g);
+        if (rr == 0.0) {  // split: recover and restart the sweep
+          __syncwarp();
+          if (lane == 0) {
+            e[i + 1] = 0.0;
+            d[i + 1] -= shift_acc;
+            e[m] = 0.0;
+          }
+          __syncwarp();
+          deflated = true;
+          break;
+        }
+        const double rinv = rsqrt(rr);
+        r = rr * rinv;
+        sn = f * rinv;
+        cs = g * rinv;
+        g = d[i + 1] - shift_acc;
+        r = (d[i] - g) * sn + 2.0 * cs * bb;
+        shift_acc = sn * r;
+        const double dnew = g + shift_acc;
+        g = cs * r - bb;
+        __syncwarp();
+        if (lane == 0) {
+          e[i + 1] = rr * rinv;
+          d[i + 1] = dnew;
+        }
+        __syncwarp();
+        // the same rotation on columns i, i + 1 of this lane's rows of Z
+        for (int row = lane; row < k; row += 32) {
+          double *zr = Zb + (size_t)row * k;
+          const double zi = zr[i], zu = zr[i + 1];
+          zr[i + 1] = sn * zi + cs * zu;
+          zr[i] = cs * zi - sn * zu;
+        }
+      }
+      if (deflated) continue;
+      __syncwarp();
+      if (lane == 0) {
+        d[l] -= shift_acc;
+        e[l] = g;
+        e[m] = 0.0;
+      }
+      __syncwarp();
+    }
+  }
+  // ascending order: permutation by insertion sort (lane 0), then a gather of
+  // the columns into S
+  if (lane == 0) {
+    for (int i = 0; i < k; ++i) perm[i] = i;
+    for (int i = 1; i < k; ++i) {
+      const int pi = perm[i];
+      const double dv = d[pi];
+      int j = i - 1;
+      while (j >= 0 && d[perm[j]] > dv) {
+        perm[j + 1] = perm[j];
+        --j;
+      }
+      perm[j + 1] = pi;
+    }
+  }
+  __syncwarp();
+  double *Sb = S + (size_t)b * k * k;
+  for (int j = lane; j < k; j += 32) w_out[(size_t)b * k + j] = ok ? d[perm[j]] : nan("");
+  for (int row = lane; row < k; row += 32)
+    for (int j = 0; j < k; ++j) Sb[(size_t)row * k + j] = Zb[(size_t)row * k + perm[j]];
+  if (!ok && lane == 0 && status) atomicExch(status, (int)MFG_ERR_NO_CONVERGENCE);
+}
+
+int launch_tridiag_eigh_full(int64_t k, int64_t p, const double *H, double *w, double *S,
+                             double *Z, int *status, cudaStream_t s) {
+  if (p <= 0 || k <= 0) return MFG_OK;
+  const size_t smem = (size_t)2 * k * sizeof(double) + (size_t)k * sizeof(int);
+  if (smem > 48 * 1024) return MFG_ERR_UNSUPPORTED;
+  tridiag_eigh_full_kernel<<<(unsigned)p, 32, smem, s>>>((int)k, p, H, w, S, Z, status);
+  return MFG_LAUNCH_STATUS();
+}
+
 // ------------------------------------------------- divide and conquer, CTA per problem
 //
 // Cuppen's divide and conquer with every coupling torn: T = diag(T_1, T_2) +

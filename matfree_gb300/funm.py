@@ -180,6 +180,21 @@ def tridiag_eigh_first(H: torch.Tensor):
     return lam, fsq
 
 
+def tridiag_eigh(H: torch.Tensor):
+    """Eigenvalues (ascending, (p, k)) and eigenvectors (columns of (p, k, k)) of
+    the tridiagonal part of (H + H^T)/2 for a stack H (p, k, k) float64."""
+    p, k, _ = H.shape
+    H = H.contiguous()
+    w = torch.empty((p, k), dtype=torch.float64, device=H.device)
+    S = torch.empty((p, k, k), dtype=torch.float64, device=H.device)
+    Z = torch.empty((p, k, k), dtype=torch.float64, device=H.device)
+    st = _lib.lib().mfg_tridiag_eigh(k, p, ctypes.c_void_p(H.data_ptr()), ctypes.c_void_p(w.data_ptr()),
+                                     ctypes.c_void_p(S.data_ptr()), ctypes.c_void_p(Z.data_ptr()),
+                                     stream_ptr())
+    _lib.check(st, "mfg_tridiag_eigh")
+    return w, S
+
+
 def monte_carlo_funm_sym(dense_funm, tridiag_sym, /):
     """matfree/funm.py:205-243."""
     return MonteCarloFunmSym(dense_funm, tridiag_sym)

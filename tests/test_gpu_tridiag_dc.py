@@ -4,7 +4,8 @@ otherwise) against numpy's eigh on hard spectra (needs a GPU).
 Eigenvalues agree to 1e-12 of the spectral radius.  Eigenvector first
 components are compared through quadratures sum_i g(lambda_i) s_1i^2, which
 do not depend on the choice of basis inside a degenerate eigenspace; the
-weights sum to one to 1e-12.
+weights sum to one to 1e-12.  The full-eigenvector solver (mfg_tridiag_eigh)
+is checked through S^T S = I and S diag(w) S^T = T to 1e-12 k.
 """
 
 import numpy as np
@@ -127,3 +128,20 @@ def test_log_quadrature_of_lanczos_tridiagonals(k):
         w0, S0 = np.linalg.eigh(H[b])
         want = np.sum(np.log(w0) * S0[0] ** 2)
         assert abs(got[b] - want) <= 1e-10 * max(abs(want), 1.0)
+
+
+@pytest.mark.parametrize("k", [1, 2, 17, 48, 100])
+def test_tridiag_eigh_full_vectors(k):
+    # mfg_tridiag_eigh: every eigenvector (the derivative of e1^T f(T) e1 uses them)
+    rng = np.random.default_rng(2000 + k)
+    kinds = KINDS if k > 2 else ["normal", "wilkinson", "zero"]
+    cases = [_case(kind, k, rng) for kind in kinds] if k > 1 else [(rng.standard_normal(1), np.zeros(0))]
+    H = _stack(cases)
+    w, S = mf.funm.tridiag_eigh(torch.as_tensor(H, device="cuda"))
+    w, S = w.cpu().numpy(), S.cpu().numpy()
+    for b in range(len(cases)):
+        T = H[b]
+        scale = max(np.abs(np.linalg.eigvalsh(T)).max(), 1e-300)
+        np.testing.assert_allclose(w[b], np.linalg.eigvalsh(T), rtol=0, atol=1e-12 * scale)
+        np.testing.assert_allclose(S[b].T @ S[b], np.eye(k), atol=1e-12 * k)
+        np.testing.assert_allclose((S[b] * w[b]) @ S[b].T, T, atol=1e-12 * k * scale)
