@@ -579,6 +579,122 @@ bool tcgen05_supported_shape(int64_t n, int64_t p) {
   return n > 0 && p > 0 && n < (1ll << 31) && p < (1ll << 31) && encode_fn() != nullptr;
 }
 
+// ---------------------------------------------------------------------------
+// Few right-hand sides (p <= 8, e.g. the one CG solve of a GP log-density):
+// the product is a stream of the operator, so it runs on the CUDA cores as a
+// GEMV over all SMs instead of as 128-row tensor-core tiles (n / 128 CTAs,
+// too few to draw HBM bandwidth).  One warp per operator row, 16-byte loads
+// of A_hi / A_lo and of the bf16 panel, float sums of the same three products
+// (hi hi + hi lo + lo hi), a fixed-order warp butterfly per probe.
+// ---------------------------------------------------------------------------
+
+constexpr int kGemvWarps = 8;
+
+__device__ __forceinline__ void bf16x8_to_float(const uint4 &u, float (&f)[8]) {
+  const uint32_t w[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    f[2 * i] = __uint_as_float(w[i] << 16);
+    f[2 * i + 1] = __uint_as_float(w[i] & 0xFFFF0000u);
+  }
+}
+
+template <int P, bool kSplit>
+__global__ void __launch_bounds__(32 * kGemvWarps)
+dense_gemv_kernel(const __nv_bfloat16 *__restrict__ Ahi, const __nv_bfloat16 *__restrict__ Alo,
+                  int64_t lda, const __nv_bfloat16 *__restrict__ Vhi,
+                  const __nv_bfloat16 *__restrict__ Vlo, int64_t ldvb,
+                  const float *__restrict__ Vf, int64_t ldvf, float *__restrict__ W, int64_t ldw,
+                  int n, int p, float shift) {
+  const int lane = threadIdx.x & 31;
+  const int64_t m = (int64_t)blockIdx.x * kGemvWarps + (threadIdx.x >> 5);
+  if (m >= n) return;  // warp-uniform
+  const __nv_bfloat16 *ah = Ahi + m * lda;
+  const __nv_bfloat16 *al = kSplit ? Alo + m * lda : nullptr;
+  float acc[P];
+#pragma unroll
+  for (int b = 0; b < P; ++b) acc[b] = 0.f;
+  const int n8 = n & ~7;
+  for (int c = lane * 8; c < n8; c += 256) {
+    float a1[8], a2[8];
+    bf16x8_to_float(__ldg(reinterpret_cast<const uint4 *>(ah + c)), a1);
+    if (kSplit) bf16x8_to_float(__ldg(reinterpret_cast<const uint4 *>(al + c)), a2);
+#pragma unroll
+    for (int b = 0; b < P; ++b) {
+      if (b >= p) break;
+      float v1[8], v2[8];
+      bf16x8_to_float(__ldg(reinterpret_cast<const uint4 *>(Vhi + b * ldvb + c)), v1);
+      if (kSplit) bf16x8_to_float(__ldg(reinterpret_cast<const uint4 *>(Vlo + b * ldvb + c)), v2);
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        acc[b] = fmaf(a1[t], v1[t], acc[b]);
+        if (kSplit) {
+          acc[b] = fmaf(a1[t], v2[t], acc[b]);
+          acc[b] = fmaf(a2[t], v1[t], acc[b]);
+        }
+      }
+    }
+  }
+  for (int c = n8 + lane; c < n; c += 32) {  // columns past the last multiple of 8
+    const float x1 = __bfloat162float(ah[c]);
+    const float x2 = kSplit ? __bfloat162float(al[c]) : 0.f;
+#pragma unroll
+    for (int b = 0; b < P; ++b) {
+      if (b >= p) break;
+      const float y1 = __bfloat162float(Vhi[b * ldvb + c]);
+      acc[b] = fmaf(x1, y1, acc[b]);
+      if (kSplit) {
+        acc[b] = fmaf(x1, __bfloat162float(Vlo[b * ldvb + c]), acc[b]);
+        acc[b] = fmaf(x2, y1, acc[b]);
+      }
+    }
+  }
+#pragma unroll
+  for (int b = 0; b < P; ++b) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc[b] += __shfl_xor_sync(0xffffffffu, acc[b], o);
+  }
+  if (lane == 0) {
+#pragma unroll
+    for (int b = 0; b < P; ++b)
+      if (b < p) W[b * ldw + m] = fmaf(shift, __ldg(Vf + b * ldvf + m), acc[b]);
+  }
+}
+
+template <int P>
+static void launch_gemv_p(bool split, const __nv_bfloat16 *A_hi, const __nv_bfloat16 *A_lo,
+                          int64_t lda, const __nv_bfloat16 *V_hi, const __nv_bfloat16 *V_lo,
+                          int64_t ldvb, const float *Vf, int64_t ldvf, float *W, int64_t ldw,
+                          int n, int p, float shift, cudaStream_t s) {
+  const unsigned grid = (unsigned)((n + kGemvWarps - 1) / kGemvWarps);
+  if (split)
+    dense_gemv_kernel<P, true><<<grid, 32 * kGemvWarps, 0, s>>>(A_hi, A_lo, lda, V_hi, V_lo, ldvb,
+                                                                Vf, ldvf, W, ldw, n, p, shift);
+  else
+    dense_gemv_kernel<P, false><<<grid, 32 * kGemvWarps, 0, s>>>(A_hi, A_lo, lda, V_hi, V_lo, ldvb,
+                                                                 Vf, ldvf, W, ldw, n, p, shift);
+}
+
+constexpr int64_t kGemvMaxP = 8;
+
+static int launch_dense_gemv(const __nv_bfloat16 *A_hi, const __nv_bfloat16 *A_lo, int64_t lda,
+                             const __nv_bfloat16 *V_hi, const __nv_bfloat16 *V_lo, int64_t ldvb,
+                             const float *Vf, int64_t ldvf, float *W, int64_t ldw, int64_t n,
+                             int64_t p, double shift, cudaStream_t s) {
+  const bool split = A_lo != nullptr;
+  const int ni = (int)n, pi = (int)p;
+  const float sh = (float)shift;
+  if (p == 1)
+    launch_gemv_p<1>(split, A_hi, A_lo, lda, V_hi, V_lo, ldvb, Vf, ldvf, W, ldw, ni, pi, sh, s);
+  else if (p == 2)
+    launch_gemv_p<2>(split, A_hi, A_lo, lda, V_hi, V_lo, ldvb, Vf, ldvf, W, ldw, ni, pi, sh, s);
+  else if (p <= 4)
+    launch_gemv_p<4>(split, A_hi, A_lo, lda, V_hi, V_lo, ldvb, Vf, ldvf, W, ldw, ni, pi, sh, s);
+  else
+    launch_gemv_p<8>(split, A_hi, A_lo, lda, V_hi, V_lo, ldvb, Vf, ldvf, W, ldw, ni, pi, sh, s);
+  return MFG_LAUNCH_STATUS();
+}
+
 int launch_dense_tcgen05(const __nv_bfloat16 *A_hi, const __nv_bfloat16 *A_lo, int64_t lda,
                          const __nv_bfloat16 *V_hi, const __nv_bfloat16 *V_lo, int64_t ldvb,
                          const float *Vf, int64_t ldvf, float *W, int64_t ldw, int64_t n, int64_t p,
@@ -589,6 +705,8 @@ int launch_dense_tcgen05(const __nv_bfloat16 *A_hi, const __nv_bfloat16 *A_lo, i
   if (split && V_lo == nullptr) return MFG_ERR_BAD_ARG;
   if (lda % 8 != 0 || ldvb % 8 != 0 || ((uintptr_t)A_hi & 15) || ((uintptr_t)V_hi & 15))
     return MFG_ERR_BAD_ARG;
+  if (p <= kGemvMaxP)
+    return launch_dense_gemv(A_hi, A_lo, lda, V_hi, V_lo, ldvb, Vf, ldvf, W, ldw, n, p, shift, s);
   // probes per tile: a multiple of 16 in [16, 256]
   const int64_t pt = p < 256 ? p : 256;
   const int BN = (int)((pt + 15) / 16 * 16);
