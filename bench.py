@@ -364,8 +364,8 @@ def gpu_arm(args):
 
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from one ncu
 # capture of that exact launch: --set full on `--config rbf16k4` (the same operator and
-# panel as rbf16k), kernel dense_tcgen05_pair_kernel<1>: 1.107433 GB read + 3.28 MB written.
-TRAFFIC = {("rbf16k", "bf16x3", "operator apply"): 1.107433e9 + 3.27936e6}
+# panel as rbf16k), kernel dense_tcgen05_pair_kernel<1>: 1.107385 GB read + 3.65 MB written.
+TRAFFIC = {("rbf16k", "bf16x3", "operator apply"): 1.107385e9 + 3.649536e6}
 
 
 def _two_sweep(args, prob):
