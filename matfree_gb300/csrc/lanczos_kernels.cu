@@ -596,8 +596,8 @@ stream_sweep_kernel(const __grid_constant__ CUtensorMap qmap, const T *__restric
 
   if (warp == kSWarps) {
     // copy warp: chunk t of this CTA goes into buffer t % nbuf once the row
-    // warps have released that buffer's previous chunk; lane c issues
-    // copies c, c + 32, ...
+    // warps have released that buffer's previous chunk; lane cp issues
+    // copies cp, cp + 32, ... of a chunk
     int issued = 0;
     const int ncopies = full + (ncols - full * kSPGroup) + kNV;
     // position of chunk t: probe b, row chunk c, buffer u used for the
@@ -626,19 +626,19 @@ stream_sweep_kernel(const __grid_constant__ CUtensorMap qmap, const T *__restric
                      : "memory");
       __syncwarp();
       T *dst = bufs + u * bstr;
-      for (int c = lane; c < ncopies; c += 32) {
-        if (c < full) {
-          const int x = (int)r0, y = (int)(b * kcols + coff + c * kSPGroup);
+      for (int cp = lane; cp < ncopies; cp += 32) {
+        if (cp < full) {
+          const int x = (int)r0, y = (int)(b * kcols + coff + cp * kSPGroup);
           asm volatile(
               "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes "
-              "[%0], [%1, {%3, %4}], [%2];" ::"r"(smem_addr(dst + (size_t)c * kSPGroup * kSR)),
+              "[%0], [%1, {%3, %4}], [%2];" ::"r"(smem_addr(dst + (size_t)cp * kSPGroup * kSR)),
               "l"(reinterpret_cast<uint64_t>(&qmap)), "r"(smem_addr(&full_bar[u])), "r"(x), "r"(y)
               : "memory");
         } else {
           // a tail vector, or (last kNV copies) the chunk's rows of w and of
           // the second vector
-          const int i = full * kSPGroup + (c - full);
-          const int vec = c - (ncopies - kNV);  // 0: w, 1: second vector, < 0: basis
+          const int i = full * kSPGroup + (cp - full);
+          const int vec = cp - (ncopies - kNV);  // 0: w, 1: second vector, < 0: basis
           const T *src = vec == 0   ? Wv + b * w_bstride + r0
                          : vec == 1 ? Wv2 + b * w2_bstride + r0
                                     : Q + b * q_bstride + (int64_t)(coff + i) * q_istride + r0;
