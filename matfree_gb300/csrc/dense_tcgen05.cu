@@ -385,7 +385,12 @@ dense_tcgen05_pair_kernel(const __grid_constant__ CUtensorMap map_ahi,
   const int m0 = (int)(blockIdx.x >> 1) * (2 * kBM) + (int)rank * kBM;
   const int b0 = blockIdx.y * BN;
   const int bh = b0 + (int)rank * (BN / 2);
-  const int num_k = (n + kBK - 1) / kBK;
+  // K slices of this CTA: all of them, or one half when the grid splits K
+  // (gridDim.z = 2; the two partial products then add into a zeroed W)
+  const int num_k_all = (n + kBK - 1) / kBK;
+  const int kb0 = (int)((int64_t)num_k_all * blockIdx.z / gridDim.z);
+  const int num_k = (int)((int64_t)num_k_all * (blockIdx.z + 1) / gridDim.z) - kb0;
+  const bool split_k = gridDim.z > 1;
   volatile int *abort_flag = &sh->abort;
 
   if (threadIdx.x == 0) {
@@ -423,7 +428,7 @@ dense_tcgen05_pair_kernel(const __grid_constant__ CUtensorMap map_ahi,
         uint8_t *st = tiles + (size_t)s * stage_bytes;
         const uint32_t full_s = full0_lead + (uint32_t)(s * sizeof(uint64_t));
         if (lead) mbar_arrive_expect_tx(&sh->full[s], 2u * stage_bytes);
-        const int kx = kt * kBK;
+        const int kx = (kb0 + kt) * kBK;
         tma_load_2d_pair(st, &map_ahi, full_s, kx, m0);
         tma_load_2d_pair(st + a_bytes, &map_bhi, full_s, kx, bh);
         if (kSplit) {
@@ -485,7 +490,8 @@ dense_tcgen05_pair_kernel(const __grid_constant__ CUtensorMap map_ahi,
 #pragma unroll
       for (int j = 0; j < 16; ++j) {
         const int b = b0 + c + j;
-        dst[j] = (shift != 0.f && m < n && b < p) ? __ldg(Vf + (int64_t)b * ldvf + m) : 0.f;
+        dst[j] = (shift != 0.f && blockIdx.z == 0 && m < n && b < p) ? __ldg(Vf + (int64_t)b * ldvf + m)
+                                                                      : 0.f;
       }
     };
     load_shift(0, sv);
@@ -500,7 +506,14 @@ dense_tcgen05_pair_kernel(const __grid_constant__ CUtensorMap map_ahi,
 #pragma unroll
           for (int j = 0; j < 16; ++j) {
             const int b = b0 + c + j;
-            if (b < p) W[(int64_t)b * ldw + m] = fmaf(shift, sv[j], v[j]);
+            if (b < p) {
+              const float out = fmaf(shift, sv[j], v[j]);
+              // two partial products: a two-term sum is the same in either order
+              if (split_k)
+                atomicAdd(W + (int64_t)b * ldw + m, out);
+              else
+                W[(int64_t)b * ldw + m] = out;
+            }
           }
         }
 #pragma unroll
@@ -735,9 +748,25 @@ int launch_dense_tcgen05(const __nv_bfloat16 *A_hi, const __nv_bfloat16 *A_lo, i
     mblo = mbhi;
   }
   if (pair) {
-    // grid.x: two CTAs per 256-row tile (the cluster dimension)
+    // grid.x: two CTAs per 256-row tile (the cluster dimension).  When the
+    // tiles cover fewer than 60 % of the SMs (e.g. n = 8192: 64 CTAs), each
+    // CTA streams its rows at a fixed rate and the SMs idle, so K is split in
+    // two halves (grid.z) whose partial products add into a zeroed W.
     dim3 grid((unsigned)(2 * ((n + 2 * kBM - 1) / (2 * kBM))), (unsigned)((p + BN - 1) / BN));
     if (grid.y > 65535) return MFG_ERR_UNSUPPORTED;
+    static int sms = 0;
+    if (sms == 0) {
+      int dev = 0;
+      if (cudaGetDevice(&dev) != cudaSuccess ||
+          cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        sms = 152;
+    }
+    const int num_k_all = (int)((n + kBK - 1) / kBK);
+    if ((int64_t)grid.x * grid.y * 5 < (int64_t)sms * 3 && num_k_all >= 4 * stages) {
+      grid.z = 2;
+      MFG_CUDA_TRY(cudaMemset2DAsync(W, (size_t)ldw * sizeof(float), 0, (size_t)n * sizeof(float),
+                                     (size_t)p, s));
+    }
     if (split) {
       MFG_CUDA_TRY(cudaFuncSetAttribute(dense_tcgen05_pair_kernel<true>,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
