@@ -1082,7 +1082,9 @@ int launch_proj(const T *Q, int64_t q_bstride, int64_t q_istride, int ncols, con
                 double *out, int64_t out_bstride, int64_t out_istride, cudaStream_t s,
                 int *status) {
   if (ncols <= 0 || p <= 0) return MFG_OK;
-  if (stream_sweep_buffers<T>(ncols) > 0) {
+  // the streamed sweep pays a fixed cost per launch that only pays off over
+  // enough row chunks (e.g. not for one CG vector of 8192 rows)
+  if (stream_sweep_buffers<T>(ncols) > 0 && p * ceil_div(n, (int64_t)kSR) >= 256) {
     const StreamArgs a{Q,        q_bstride, q_istride,   ncols,       nullptr, 0,   0,
                        const_cast<T *>(Wv), w_bstride,   n,           p,       partials,
                        counters, out,       out_bstride, out_istride, nullptr, 0,   status};
