@@ -822,7 +822,7 @@ static int run_cg(const mfg_operator *op, int64_t p, const T *B, T *X, int64_t l
   MFG_LAUNCH(MFG_PROF_OTHER, 4.0 * vecb, 2.0 * vecb / sizeof(T),
              launch_cg_init<T>(B, X, R, P, ld, n, p, hi, lo, partials, counters, tol * tol,
                                atol * atol, rs[0], thr, iters, s));
-  for (int64_t it = 0; it < maxiter; ++it) {
+  auto iteration = [&](int64_t it) -> int {
     double *rc = rs[it & 1], *rn = rs[(it + 1) & 1];
     MFG_CUDA_TRY(cudaMemsetAsync(nactive, 0, sizeof(int), s));
     MFG_LAUNCH(MFG_PROF_APPLY, ab, af, apply_op<T>(op, P, ld, W, ld, p, hi, lo, ld, nullptr, status, s));
@@ -833,14 +833,52 @@ static int run_cg(const mfg_operator *op, int64_t p, const T *B, T *X, int64_t l
                                    nactive, iters, s));
     MFG_LAUNCH(MFG_PROF_SCALE, 3.0 * vecb, 2.0 * vecb / sizeof(T),
                launch_cg_direction<T>(P, R, ld, n, p, rc, rn, thr, hi, lo, s));
-    // test for convergence every kCgCheckEvery iterations (and at the end):
-    // a finished row only runs frozen (alpha = 0) iterations until then
-    if ((it + 1) % kCgCheckEvery != 0 && it + 1 < maxiter) continue;
+    return MFG_OK;
+  };
+  // Iterations run in blocks of kCgCheckEvery between convergence tests (a
+  // finished row only runs frozen, alpha = 0, iterations until then).  A full
+  // block's launches are captured once as a CUDA graph and replayed, which
+  // removes the launch gaps between the small kernels of an iteration (the
+  // launch counters then count a block's launches once).  Not for callback
+  // operators (host code) or while launches are being timed.
+  const bool graphs = !prof().timing && op->kind != MFG_OP_CALLBACK;
+  cudaGraphExec_t exec = nullptr;
+  bool capture_failed = false;
+  int rc_loop = MFG_OK;
+  for (int64_t it = 0; it < maxiter;) {
+    const int64_t blk = maxiter - it < kCgCheckEvery ? maxiter - it : kCgCheckEvery;
+    bool done = false;
+    if (graphs && !capture_failed && blk == kCgCheckEvery) {
+      if (!exec) {
+        capture_failed = true;
+        if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+          int st = MFG_OK;
+          for (int64_t t = 0; t < blk && st == MFG_OK; ++t) st = iteration(it + t);
+          cudaGraph_t g = nullptr;
+          const cudaError_t ec = cudaStreamEndCapture(s, &g);
+          if (st == MFG_OK && ec == cudaSuccess && g &&
+              cudaGraphInstantiate(&exec, g, 0) == cudaSuccess)
+            capture_failed = false;
+          if (g) cudaGraphDestroy(g);
+        }
+        (void)cudaGetLastError();  // a failed capture leaves nothing queued: run eagerly
+      }
+      if (exec && cudaGraphLaunch(exec, s) == cudaSuccess) done = true;
+    }
+    for (int64_t t = 0; !done && t < blk && rc_loop == MFG_OK; ++t) rc_loop = iteration(it + t);
+    if (rc_loop != MFG_OK) break;
+    it += blk;
     int host_active = 0;
-    MFG_CUDA_TRY(cudaMemcpyAsync(&host_active, nactive, sizeof(int), cudaMemcpyDeviceToHost, s));
-    MFG_CUDA_TRY(cudaStreamSynchronize(s));
+    if (cudaMemcpyAsync(&host_active, nactive, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess) {
+      rc_loop = cuda_status(cudaGetLastError(), __FILE__, __LINE__);
+      if (rc_loop == MFG_OK) rc_loop = MFG_ERR_CUDA;
+      break;
+    }
     if (host_active == 0) break;
   }
+  if (exec) cudaGraphExecDestroy(exec);
+  if (rc_loop != MFG_OK) return rc_loop;
   int host_status = 0;
   MFG_CUDA_TRY(cudaMemcpyAsync(&host_status, status, sizeof(int), cudaMemcpyDeviceToHost, s));
   MFG_CUDA_TRY(cudaStreamSynchronize(s));
