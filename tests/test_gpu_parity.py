@@ -320,8 +320,11 @@ def test_funm_lanczos_sym_logm_vector():
 @pytest.mark.parametrize("precision,tol", [("bf16x3", 5e-5), ("bf16", 1.5e-2)])
 @pytest.mark.parametrize("n,p", [(64, 16), (200, 1), (300, 100), (1000, 256), (777, 300),
                                  # CTA-pair (2-SM) form: even and ragged 256-row tiles,
-                                 # one and two probe tiles, a probe tile of 64
-                                 (1024, 256), (1500, 256), (2600, 300), (1300, 64), (1100, 40)])
+                                 # one and two probe tiles, a probe tile of 64; the
+                                 # first three also split K over two CTAs
+                                 (1024, 256), (1500, 256), (2600, 300), (1300, 64), (1100, 40),
+                                 # GEMV form (p <= 8): ragged column tails, 5 and 8 probes
+                                 (203, 1), (1001, 5), (4099, 8)])
 def test_dense_tensor_core_apply(precision, tol, n, p):
     rng = np.random.default_rng(n + p)
     A = rng.standard_normal((n, n)) / np.sqrt(n)
