@@ -1,0 +1,206 @@
+"""A scalar restatement of the divide-and-conquer quadrature kernel
+(tridiag_dc_kernel: the same torn leaves, merge levels, deflation, secular
+iteration, Loewner vectors and merge order) against numpy's eigh.  No GPU.
+
+It checks the algorithm the kernel implements on the CPU: eigenvalues to
+1e-12 of the spectral radius and Gauss quadratures sum_i g(lambda_i) s_1i^2 to
+1e-12 on Gaussian, Wilkinson, glued, split, tiny-coupling and zero
+tridiagonals.
+"""
+
+import math
+
+import numpy as np
+import pytest
+
+EPS = np.finfo(np.float64).eps
+
+
+def _quad_root(c, P1, P2, s1, s2):
+    # root in (P1, P2) of c + s1/(P1 - x) + s2/(P2 - x) = 0
+    a1 = c * (P1 + P2) + s1 + s2
+    a0 = c * P1 * P2 + s1 * P2 + s2 * P1
+    sq = math.sqrt(max(a1 * a1 - 4.0 * c * a0, 0.0))
+    return 2.0 * a0 / (a1 + sq) if a1 > 0 else (a1 - sq) / (2.0 * c)
+
+
+def _quad_step(c, A, B, s1, s2, f):
+    a1 = c * (A + B) + s1 + s2
+    a0 = A * B * f
+    sq = math.sqrt(max(a1 * a1 - 4.0 * c * a0, 0.0))
+    if a1 > 0:
+        return 2.0 * a0 / (a1 + sq)
+    return (a1 - sq) / (2.0 * c) if c != 0 else math.nan
+
+
+def _quad_step_right(c, A0, A, s0, s1, f):
+    a1 = c * (A0 + A) + s0 + s1
+    a0 = A0 * A * f
+    sq = math.sqrt(max(a1 * a1 - 4.0 * c * a0, 0.0))
+    return (a1 + sq) / (2.0 * c) if a1 >= 0 else 2.0 * a0 / (a1 - sq)
+
+
+def _secular(P, ZZ, mk, j, rho, upper):
+    """Root j as (offset x, origin o); the kernel's dc_secular_root."""
+    ir = 1.0 / rho
+    last = j + 1 >= mk
+    lo_pole = P[j]
+    hi_pole = upper if last else P[j + 1]
+    xma = 0.5 * (lo_pole + hi_pole)
+    fmid = ir + sum(ZZ[i] / (P[i] - xma) for i in range(mk))
+    zzj, zzj1 = ZZ[j], (0.0 if last else ZZ[j + 1])
+    two_below = last and mk > 1
+    zzjm = ZZ[j - 1] if two_below else 0.0
+    o = j + 1 if (not last and fmid < 0.0) else j
+    base = P[o]
+    lo, hi = lo_pole - base, hi_pole - base
+    P1 = P[j] - base
+    P2 = hi if last else P[j + 1] - base
+    P0 = P[j - 1] - base if two_below else 0.0
+    xm = 0.5 * (lo + hi)
+    if mk == 1:
+        x = rho * zzj
+    elif last:
+        c = fmid - zzj / (P[j] - xma) - zzjm / (P[j - 1] - xma)
+        x = xm + _quad_step_right(c, P0 - xm, P1 - xm, zzjm, zzj, fmid) if c > 0 else xm
+    else:
+        c = fmid - zzj / (P[j] - xma) - zzj1 / (P[j + 1] - xma)
+        x = _quad_root(c, P1, P2, zzj, zzj1)
+    if not (lo < x < hi):
+        x = xm
+    m0, m1 = (j - 1 if two_below else j), (j if last else j + 1)
+    for _ in range(128):
+        rs = drs = ab = 0.0
+        for i in range(mk):
+            if m0 <= i <= m1:
+                continue
+            inv = 1.0 / ((P[i] - base) - x)
+            t = ZZ[i] * inv
+            rs += t
+            drs += t * inv
+            ab += abs(t)
+        A, B, A0 = P1 - x, P2 - x, P0 - x
+        tj = zzj / A
+        tj1 = 0.0 if last else zzj1 / B
+        tjm = zzjm / A0 if two_below else 0.0
+        f = ir + rs + tj + tj1 + tjm
+        sab = ab + abs(tj) + abs(tj1) + abs(tjm)
+        if f > 0:
+            hi = x
+        else:
+            lo = x
+        if abs(f) <= EPS * mk * (ir + sab) or hi - lo <= 2.0 * EPS * max(abs(lo), abs(hi)):
+            return x, o, True
+        if last and mk == 1:
+            eta = A + zzj * rho
+        elif last:
+            c = ir + rs - drs * A0
+            eta = _quad_step_right(c, A0, A, zzjm + drs * A0 * A0, zzj, f) if c > 0 else math.nan
+        elif o == j:
+            eta = _quad_step(ir + rs - drs * B, A, B, zzj, zzj1 + drs * B * B, f)
+        else:
+            eta = _quad_step(ir + rs - drs * A, A, B, zzj + drs * A * A, zzj1, f)
+        if abs(eta) <= 2.0 * EPS * abs(x):
+            return x, o, True
+        xn = x + eta
+        x = xn if lo < xn < hi else 0.5 * (lo + hi)
+    return x, o, False
+
+
+def dc_first_rows(d, e):
+    """Eigenvalues (ascending) and squared first eigenvector components."""
+    k = len(d)
+    LAM = np.array([d[i] - (e[i - 1] if i > 0 else 0.0) - (e[i] if i + 1 < k else 0.0) for i in range(k)])
+    FR, LR = np.ones(k), np.ones(k)
+    ok = True
+    w = 1
+    while w < k:
+        for a in range(0, k - w, 2 * w):  # merges of this level
+            mid, hi = a + w, min(a + 2 * w, k)
+            rho = e[mid - 1]
+            sg = -1.0 if rho < 0 else 1.0
+            rho = abs(rho)
+            tol = 8.0 * EPS * max(abs(LAM[a]), abs(LAM[mid - 1]), abs(LAM[mid]), abs(LAM[hi - 1]), 2.0 * rho)
+            # sorted merge of the halves (negated when rho < 0), with deflation
+            items = [(sg * LAM[i], LR[i], FR[i], 0.0) for i in range(a, mid)]
+            items += [(sg * LAM[i], FR[i], 0.0, LR[i]) for i in range(mid, hi)]
+            items.sort(key=lambda t: t[0])
+            D, Z, F, L, dfl = [], [], [], [], []
+            zs = 0.0
+            for dv, z, f, l in items:
+                if rho * abs(z) <= tol:
+                    dfl.append((dv, f, l))
+                    continue
+                zs += z * z
+                if D and dv - D[-1] <= tol:  # close poles: rotate, drop the earlier
+                    r = math.hypot(Z[-1], z)
+                    c, s = z / r, Z[-1] / r
+                    dfl.append((D[-1], c * F[-1] - s * f, c * L[-1] - s * l))
+                    D[-1], Z[-1], F[-1], L[-1] = dv, r, s * F[-1] + c * f, s * L[-1] + c * l
+                else:
+                    D.append(dv), Z.append(z), F.append(f), L.append(l)
+            dfl.sort(key=lambda t: t[0])
+            mk = len(D)
+            out = []
+            if mk:
+                upper = D[-1] + rho * zs * (1.0 + 16.0 * EPS) + 16.0 * EPS * abs(D[-1])
+                ZZ = [z * z for z in Z]
+                roots = []
+                for j in range(mk):
+                    x, o, conv = _secular(D, ZZ, mk, j, rho, upper)
+                    ok &= conv
+                    roots.append((x, o))
+                zh = []
+                for i in range(mk):  # Loewner
+                    prod = ((D[roots[mk - 1][1]] - D[i]) + roots[mk - 1][0]) / rho
+                    for j in range(mk - 1):
+                        prod *= ((D[roots[j][1]] - D[i]) + roots[j][0]) / (D[j if j < i else j + 1] - D[i])
+                    zh.append(math.copysign(math.sqrt(max(prod, 0.0)), Z[i]))
+                for j in range(mk):
+                    x, o = roots[j]
+                    u = np.array([zh[i] / ((D[i] - D[o]) - x) for i in range(mk)])
+                    u /= np.linalg.norm(u)
+                    out.append((D[o] + x, float(np.dot(F, u)), float(np.dot(L, u))))
+            merged = sorted(out + dfl, key=lambda t: t[0])
+            if sg < 0:
+                merged = [(-v, f, l) for v, f, l in reversed(merged)]
+            for t, (v, f, l) in enumerate(merged):
+                LAM[a + t], FR[a + t], LR[a + t] = v, f, l
+        w *= 2
+    return LAM, FR * FR, ok
+
+
+def _case(kind, k, rng):
+    if kind == "normal":
+        return rng.standard_normal(k), rng.standard_normal(k - 1)
+    if kind == "wilkinson":
+        return np.abs(np.arange(k) - k // 2).astype(float), np.ones(k - 1)
+    if kind == "glued":
+        d = np.resize(np.abs(np.arange(7) - 3).astype(float), k)
+        e = np.ones(k - 1)
+        e[6::7] = 1e-10
+        return d, e
+    if kind == "split":
+        e = np.zeros(k - 1)
+        e[::3] = 1.0
+        return np.ones(k), e
+    if kind == "tiny":
+        return rng.standard_normal(k), rng.standard_normal(k - 1) * 10.0 ** rng.integers(-18, 0, k - 1)
+    if kind == "negative":
+        return rng.uniform(1, 3, k), -rng.uniform(0.1, 0.5, k - 1)
+    return np.zeros(k), np.zeros(k - 1)
+
+
+@pytest.mark.parametrize("kind", ["normal", "wilkinson", "glued", "split", "tiny", "negative", "zero"])
+@pytest.mark.parametrize("k", [1, 2, 5, 16, 17, 33])
+def test_dc_model_matches_eigh(kind, k):
+    rng = np.random.default_rng(100 * sum(map(ord, kind)) + k)
+    d, e = _case(kind, k, rng) if k > 1 else (rng.standard_normal(1), np.zeros(0))
+    T = np.diag(d) + np.diag(e, 1) + np.diag(e, -1)
+    w0, S0 = np.linalg.eigh(T)
+    lam, fsq, ok = dc_first_rows(d, e)
+    assert ok
+    scale = max(np.abs(w0).max(), 1e-300)
+    np.testing.assert_allclose(lam, w0, rtol=0, atol=1e-12 * scale)
+    for g in (lambda x: np.exp(-x / scale), lambda x: np.sin(3 * x / scale)):
+        assert abs(np.sum(g(lam) * fsq) - np.sum(g(w0) * S0[0] ** 2)) <= 1e-12
