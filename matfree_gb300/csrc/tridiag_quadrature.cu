@@ -156,11 +156,12 @@ __global__ void tridiag_ql_kernel(int k, int64_t p, const double *__restrict__ H
 //
 // Eigenvalues (ascending) and the full eigenvector matrix of each T, for the
 // derivative of e1^T f(T) e1 (the Daleckii-Krein form needs every
-// eigenvector).  Implicit QL with Wilkinson shifts as above; every lane of
-// the warp runs the same shift chase on the warp's d, e (identical
-// arithmetic, so identical values), and applies each rotation to its own rows
-// of Z (rows lane, lane + 32, ...).  Z (scratch) is row-major k x k; the
-// sorted eigenvectors go to S as columns (S[r][j] = component r of vector j).
+// eigenvector).  Implicit QL with Wilkinson shifts as above.  Lane 0 runs
+// each sweep's shift chase alone (inputs loaded one rotation ahead, as in the
+// first-row kernel) and records the rotations; the warp then applies them,
+// in order, to its rows of Z (rows lane, lane + 32, ...).  Z (scratch) is
+// row-major k x k; the sorted eigenvectors go to S as columns
+// (S[r][j] = component r of vector j).
 
 __global__ void tridiag_eigh_full_kernel(int k, int64_t p, const double *__restrict__ H,
                                          double *__restrict__ w_out, double *__restrict__ S,
@@ -171,7 +172,9 @@ __global__ void tridiag_eigh_full_kernel(int k, int64_t p, const double *__restr
   if (b >= p) return;
   double *d = smf;
   double *e = d + k;
-  int *perm = reinterpret_cast<int *>(e + k);
+  double *rc = e + k;   // rotation i of the current sweep: cosine
+  double *rs = rc + k;  // and sine
+  int *perm = reinterpret_cast<int *>(rs + k);
   const double *Hb = H + (size_t)b * k * k;
   double *Zb = Z + (size_t)b * k * k;
   for (int i = lane; i < k; i += 32) {
@@ -181,72 +184,93 @@ __global__ void tridiag_eigh_full_kernel(int k, int64_t p, const double *__restr
   for (int r = lane; r < k; r += 32)
     for (int c = 0; c < k; ++c) Zb[(size_t)r * k + c] = r == c ? 1.0 : 0.0;
   __syncwarp();
-  bool ok = true;
-  for (int l = 0; l < k && ok; ++l) {
+  int ok = 1;
+  for (int l = 0; l < k; ++l) {
     int sweeps = 0;
     while (true) {
-      int m = l;
-      for (; m < k - 1; ++m) {
-        const double dd = fabs(d[m]) + fabs(d[m + 1]);
-        if (fabs(e[m]) <= DBL_EPSILON * dd) break;
-      }
-      if (m == l) break;
-      if (++sweeps > kMaxSweeps) {
-        ok = false;
-        break;
-      }
-      double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
-      double r = hypot(g, 1.0);
-      g = d[m] - d[l] + e[l] / (g + copysign(r, g));
-      double sn = 1.0, cs = 1.0, shift_acc = 0.0;
-      bool deflated = false;
-      for (int i = m - 1; i >= l; --i) {
-        const double f = sn * e[i];
-        const double bb = cs * e[i];
-        const double rr = fma(f, f, g * g);
-        if (rr == 0.0) {  // split: recover and restart the sweep
-          __syncwarp();
-          if (lane == 0) {
-            e[i + 1] = 0.0;
-            d[i + 1] -= shift_acc;
+      // lane 0: one sweep of the chase; the rotations applied are i = hi_i
+      // down to lo_i (none when l has converged, or on failure)
+      int hi_i = -1, lo_i = 0, done = 0;
+      if (lane == 0) {
+        int m = l;
+        for (; m < k - 1; ++m) {
+          const double dd = fabs(d[m]) + fabs(d[m + 1]);
+          if (fabs(e[m]) <= DBL_EPSILON * dd) break;
+        }
+        if (m == l) {
+          done = 1;
+        } else if (++sweeps > kMaxSweeps) {
+          done = 1;
+          ok = 0;
+        } else {
+          double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
+          double r = hypot(g, 1.0);
+          g = d[m] - d[l] + e[l] / (g + copysign(r, g));
+          double sn = 1.0, cs = 1.0, shift_acc = 0.0;
+          bool deflated = false;
+          double d_up = d[m];
+          double e_i = e[m - 1], d_i = d[m - 1];
+          hi_i = m - 1;
+          lo_i = m;  // the last rotation applied so far
+          for (int i = m - 1; i >= l; --i) {
+            double e_nx = 0.0, d_nx = 0.0;
+            if (i > l) {
+              e_nx = e[i - 1];
+              d_nx = d[i - 1];
+            }
+            const double f = sn * e_i;
+            const double bb = cs * e_i;
+            const double rr = fma(f, f, g * g);
+            if (rr == 0.0) {  // split: recover and restart the sweep
+              e[i + 1] = 0.0;
+              d[i + 1] = d_up - shift_acc;
+              e[m] = 0.0;
+              deflated = true;
+              break;
+            }
+            const double rinv = rsqrt(rr);
+            e[i + 1] = rr * rinv;
+            sn = f * rinv;
+            cs = g * rinv;
+            g = d_up - shift_acc;
+            r = (d_i - g) * sn + 2.0 * cs * bb;
+            shift_acc = sn * r;
+            d[i + 1] = g + shift_acc;
+            g = cs * r - bb;
+            rc[i] = cs;
+            rs[i] = sn;
+            lo_i = i;
+            d_up = d_i;
+            e_i = e_nx;
+            d_i = d_nx;
+          }
+          if (!deflated) {
+            d[l] -= shift_acc;
+            e[l] = g;
             e[m] = 0.0;
           }
-          __syncwarp();
-          deflated = true;
-          break;
-        }
-        const double rinv = rsqrt(rr);
-        r = rr * rinv;
-        sn = f * rinv;
-        cs = g * rinv;
-        g = d[i + 1] - shift_acc;
-        r = (d[i] - g) * sn + 2.0 * cs * bb;
-        shift_acc = sn * r;
-        const double dnew = g + shift_acc;
-        g = cs * r - bb;
-        __syncwarp();
-        if (lane == 0) {
-          e[i + 1] = rr * rinv;
-          d[i + 1] = dnew;
-        }
-        __syncwarp();
-        // the same rotation on columns i, i + 1 of this lane's rows of Z
-        for (int row = lane; row < k; row += 32) {
-          double *zr = Zb + (size_t)row * k;
-          const double zi = zr[i], zu = zr[i + 1];
-          zr[i + 1] = sn * zi + cs * zu;
-          zr[i] = cs * zi - sn * zu;
         }
       }
-      if (deflated) continue;
-      __syncwarp();
-      if (lane == 0) {
-        d[l] -= shift_acc;
-        e[l] = g;
-        e[m] = 0.0;
+      done = __shfl_sync(0xffffffffu, done, 0);
+      hi_i = __shfl_sync(0xffffffffu, hi_i, 0);
+      lo_i = __shfl_sync(0xffffffffu, lo_i, 0);
+      __syncwarp();  // rc, rs written by lane 0
+      if (done) break;
+      // the sweep's rotations on columns (i, i + 1) of this lane's rows of Z
+      for (int row = lane; row < k; row += 32) {
+        double *zr = Zb + (size_t)row * k;
+        double zu = zr[hi_i + 1];
+        for (int i = hi_i; i >= lo_i; --i) {
+          const double zi = zr[i];
+          zr[i + 1] = rs[i] * zi + rc[i] * zu;
+          zu = rc[i] * zi - rs[i] * zu;
+        }
+        zr[lo_i] = zu;
       }
       __syncwarp();
     }
+    ok = __shfl_sync(0xffffffffu, ok, 0);
+    if (!ok) break;
   }
   // ascending order: permutation by insertion sort (lane 0), then a gather of
   // the columns into S
@@ -274,7 +298,7 @@ __global__ void tridiag_eigh_full_kernel(int k, int64_t p, const double *__restr
 int launch_tridiag_eigh_full(int64_t k, int64_t p, const double *H, double *w, double *S,
                              double *Z, int *status, cudaStream_t s) {
   if (p <= 0 || k <= 0) return MFG_OK;
-  const size_t smem = (size_t)2 * k * sizeof(double) + (size_t)k * sizeof(int);
+  const size_t smem = (size_t)4 * k * sizeof(double) + (size_t)k * sizeof(int);
   if (smem > 48 * 1024) return MFG_ERR_UNSUPPORTED;
   tridiag_eigh_full_kernel<<<(unsigned)p, 32, smem, s>>>((int)k, p, H, w, S, Z, status);
   return MFG_LAUNCH_STATUS();
