@@ -49,6 +49,11 @@ def two_sweep_applies(op, k: int) -> bool:
     return op.basis_dtype == torch.float32 and 2 <= k <= 129
 
 
+def full_reortho(op, k: int) -> str:
+    """The fastest full-reorthogonalisation form for this operator and k."""
+    return "full-two-sweep" if two_sweep_applies(op, k) else "full"
+
+
 def run_hessenberg(op, k: int, V: torch.Tensor, *, reortho: str = "full", workspace=None):
     """Batched Arnoldi over the rows of V (p, n) on the GPU.
 
@@ -135,7 +140,8 @@ class _TridiagSymFull(_Decomposition):
     def batched(self, matvec, V: torch.Tensor, *params) -> _DecompResult:
         """Decompose every row of V (p, n) at once; outputs carry a leading p axis."""
         op = as_operator(matvec, V.shape[1], V.dtype, params)
-        Q, H, r, c = run_hessenberg(op, self.num_matvecs, V, reortho="full")
+        k = self.num_matvecs
+        Q, H, r, c = run_hessenberg(op, k, V, reortho=full_reortho(op, k))
         d, e = _tridiag_from_hessenberg(H)
         out_dt = V.dtype if V.dtype in (torch.float32, torch.float64) else torch.float32
         d, e = d.to(out_dt), e.to(out_dt)
@@ -169,7 +175,9 @@ class _Hessenberg(_Decomposition):
 
     def batched(self, matvec, V: torch.Tensor, *params) -> _DecompResult:
         op = as_operator(matvec, V.shape[1], V.dtype, params)
-        Q, H, r, c = run_hessenberg(op, self.num_matvecs, V, reortho=self.reortho)
+        k = self.num_matvecs
+        mode = full_reortho(op, k) if self.reortho == "full" else self.reortho
+        Q, H, r, c = run_hessenberg(op, k, V, reortho=mode)
         out_dt = V.dtype if V.dtype in (torch.float32, torch.float64) else torch.float32
         return _DecompResult(Q_tall=Q, J_small=H.to(out_dt), residual=r, init_length_inv=c.to(out_dt))
 

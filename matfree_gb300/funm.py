@@ -20,7 +20,7 @@ import torch
 
 from . import _lib
 from ._panel import Workspace, as_panel, require_cuda, stream_ptr
-from .decomp import _flat_operator, _TridiagSymFull, run_hessenberg, two_sweep_applies
+from .decomp import _flat_operator, _TridiagSymFull, full_reortho, run_hessenberg, two_sweep_applies
 from .operators import Operator, as_operator
 from .tree import ravel_pytree
 
@@ -114,7 +114,7 @@ class MonteCarloFunmSym:
         if self.dense_funm.kind is not None:
             return slq_values(op, k, samples, self.dense_funm.kind, self.dense_funm.param)
         # arbitrary f: device Krylov + device eigensolve, f evaluated by torch on the GPU
-        _, H, _, c = run_hessenberg(op, k, samples, reortho="full")
+        _, H, _, c = run_hessenberg(op, k, samples, reortho=full_reortho(op, k))
         lam, fsq = tridiag_eigh_first(H)
         length_sq = 1.0 / (c * c)
         return length_sq * (self.dense_funm.apply_scalar(lam) * fsq).sum(-1)
