@@ -819,18 +819,28 @@ static int run_cg(const mfg_operator *op, int64_t p, const T *B, T *X, int64_t l
 
   MFG_CUDA_TRY(cudaMemsetAsync(counters, 0, (size_t)p * 4, s));
   MFG_CUDA_TRY(cudaMemsetAsync(status, 0, 16, s));
+  MFG_CUDA_TRY(cudaMemsetAsync(nactive, 0, 2 * sizeof(int), s));
   MFG_LAUNCH(MFG_PROF_OTHER, 4.0 * vecb, 2.0 * vecb / sizeof(T),
              launch_cg_init<T>(B, X, R, P, ld, n, p, hi, lo, partials, counters, tol * tol,
                                atol * atol, rs[0], thr, iters, s));
+  // Iteration it counts the rows that keep running into nactive[it & 1] and
+  // zeroes nactive[(it + 1) & 1] for the next one.
+  const bool small = n <= kCgSmallMaxN;
   auto iteration = [&](int64_t it) -> int {
     double *rc = rs[it & 1], *rn = rs[(it + 1) & 1];
-    MFG_CUDA_TRY(cudaMemsetAsync(nactive, 0, sizeof(int), s));
+    int *na = nactive + (it & 1), *na_next = nactive + ((it + 1) & 1);
     MFG_LAUNCH(MFG_PROF_APPLY, ab, af, apply_op<T>(op, P, ld, W, ld, p, hi, lo, ld, nullptr, status, s));
+    if (small) {
+      MFG_LAUNCH(MFG_PROF_SUB, 7.0 * vecb, 10.0 * vecb / sizeof(T),
+                 launch_cg_step_small<T>(X, R, P, W, ld, n, p, rc, thr, rn, na, na_next, iters,
+                                         hi, lo, s));
+      return MFG_OK;
+    }
     MFG_LAUNCH(MFG_PROF_PROJ, 2.0 * vecb, 2.0 * vecb / sizeof(T),
                launch_proj<T>(P, ld, ld, 1, W, ld, n, p, partials, counters, pap, 1, 1, s, status));
     MFG_LAUNCH(MFG_PROF_SUB, 6.0 * vecb, 6.0 * vecb / sizeof(T),
                launch_cg_update<T>(X, R, P, W, ld, n, p, rc, pap, thr, partials, counters, rn,
-                                   nactive, iters, s));
+                                   na, na_next, iters, s));
     MFG_LAUNCH(MFG_PROF_SCALE, 3.0 * vecb, 2.0 * vecb / sizeof(T),
                launch_cg_direction<T>(P, R, ld, n, p, rc, rn, thr, hi, lo, s));
     return MFG_OK;
@@ -867,9 +877,10 @@ static int run_cg(const mfg_operator *op, int64_t p, const T *B, T *X, int64_t l
     }
     for (int64_t t = 0; !done && t < blk && rc_loop == MFG_OK; ++t) rc_loop = iteration(it + t);
     if (rc_loop != MFG_OK) break;
+    const int *last_count = nactive + ((it + blk - 1) & 1);
     it += blk;
     int host_active = 0;
-    if (cudaMemcpyAsync(&host_active, nactive, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+    if (cudaMemcpyAsync(&host_active, last_count, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess) {
       rc_loop = cuda_status(cudaGetLastError(), __FILE__, __LINE__);
       if (rc_loop == MFG_OK) rc_loop = MFG_ERR_CUDA;

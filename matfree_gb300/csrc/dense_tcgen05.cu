@@ -598,10 +598,22 @@ bool tcgen05_supported_shape(int64_t n, int64_t p) {
 // GEMV over all SMs instead of as 128-row tensor-core tiles (n / 128 CTAs,
 // too few to draw HBM bandwidth).  One warp per operator row, 16-byte loads
 // of A_hi / A_lo and of the bf16 panel, float sums of the same three products
-// (hi hi + hi lo + lo hi), a fixed-order warp butterfly per probe.
+// (hi hi + hi lo + lo hi), a fixed-order warp butterfly per probe.  The
+// operator loads of the next 256 columns are issued before the current ones
+// are used (two in flight per lane) and bypass L1, which keeps the panel
+// that every warp of the SM re-reads there.
 // ---------------------------------------------------------------------------
 
 constexpr int kGemvWarps = 8;
+
+// 16 bytes of the operator, read once: not allocated in L1
+__device__ __forceinline__ uint4 ld_stream16(const __nv_bfloat16 *p) {
+  uint4 v;
+  asm volatile("ld.global.nc.L1::no_allocate.v4.u32 {%0, %1, %2, %3}, [%4];"
+               : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+               : "l"(p));
+  return v;
+}
 
 __device__ __forceinline__ void bf16x8_to_float(const uint4 &u, float (&f)[8]) {
   const uint32_t w[4] = {u.x, u.y, u.z, u.w};
@@ -628,10 +640,22 @@ dense_gemv_kernel(const __nv_bfloat16 *__restrict__ Ahi, const __nv_bfloat16 *__
 #pragma unroll
   for (int b = 0; b < P; ++b) acc[b] = 0.f;
   const int n8 = n & ~7;
+  uint4 hcur = make_uint4(0u, 0u, 0u, 0u), lcur = hcur;
+  if (lane * 8 < n8) {
+    hcur = ld_stream16(ah + lane * 8);
+    if (kSplit) lcur = ld_stream16(al + lane * 8);
+  }
   for (int c = lane * 8; c < n8; c += 256) {
+    uint4 hnext = make_uint4(0u, 0u, 0u, 0u), lnext = hnext;
+    if (c + 256 < n8) {
+      hnext = ld_stream16(ah + c + 256);
+      if (kSplit) lnext = ld_stream16(al + c + 256);
+    }
     float a1[8], a2[8];
-    bf16x8_to_float(__ldg(reinterpret_cast<const uint4 *>(ah + c)), a1);
-    if (kSplit) bf16x8_to_float(__ldg(reinterpret_cast<const uint4 *>(al + c)), a2);
+    bf16x8_to_float(hcur, a1);
+    if (kSplit) bf16x8_to_float(lcur, a2);
+    hcur = hnext;
+    lcur = lnext;
 #pragma unroll
     for (int b = 0; b < P; ++b) {
       if (b >= p) break;

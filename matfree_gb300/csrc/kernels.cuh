@@ -63,7 +63,15 @@ int launch_cg_init(const T *B, T *X, T *R, T *P, int64_t ld, int64_t n, int64_t 
 template <typename T>
 int launch_cg_update(T *X, T *R, const T *P, const T *W, int64_t ld, int64_t n, int64_t p,
                      const double *rs, const double *pap, const double *thr, double *partials,
-                     unsigned *counters, double *rs_next, int *nactive, int *iters, cudaStream_t s);
+                     unsigned *counters, double *rs_next, int *nactive, int *nactive_clear,
+                     int *iters, cudaStream_t s);
+// one CTA per probe for the whole post-product iteration of vectors up to kCgSmallMaxN
+constexpr int64_t kCgSmallMaxN = 8192;
+template <typename T>
+int launch_cg_step_small(T *X, T *R, T *P, const T *W, int64_t ld, int64_t n, int64_t p,
+                         const double *rs, const double *thr, double *rs_next, int *nactive,
+                         int *nactive_clear, int *iters, __nv_bfloat16 *hi, __nv_bfloat16 *lo,
+                         cudaStream_t s);
 template <typename T>
 int launch_cg_direction(T *P, const T *R, int64_t ld, int64_t n, int64_t p, const double *rs,
                         const double *rs_next, const double *thr, __nv_bfloat16 *hi,

@@ -1240,16 +1240,20 @@ cg_init_kernel(const T *__restrict__ B, T *__restrict__ X, T *__restrict__ R, T 
 
 // For a probe still running (rs > thr): alpha = rs / pAp, X += alpha P,
 // R -= alpha W; every probe: rs_next = ||R||^2.  The last CTA of a probe
-// counts it into *nactive when it keeps running after this iteration.
+// counts it into *nactive when it keeps running after this iteration; the
+// count alternates between two slots, and this launch zeroes the slot of the
+// next iteration (*nactive_clear).
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
 cg_update_kernel(T *__restrict__ X, T *__restrict__ R, const T *__restrict__ P,
                  const T *__restrict__ W, int64_t ld, int64_t n, const double *__restrict__ rs,
                  const double *__restrict__ pap, const double *__restrict__ thr, int nchunks,
                  double *partials, unsigned *counters, double *__restrict__ rs_next,
-                 int *__restrict__ nactive, int *__restrict__ iters) {
+                 int *__restrict__ nactive, int *__restrict__ nactive_clear,
+                 int *__restrict__ iters) {
   constexpr int VW = Vec<T>::width;
   const int64_t c = blockIdx.x, b = blockIdx.y;
+  if (c == 0 && b == 0 && threadIdx.x == 0) *nactive_clear = 0;  // the next iteration's count
   const bool active = rs[b] > thr[b];
   T r[kVPT][VW];
   load_chunk<T, false>(R + b * ld, n, c, r);
@@ -1306,6 +1310,102 @@ cg_direction_kernel(T *__restrict__ P, const T *__restrict__ R, int64_t ld, int6
   if (hi) store_split<T>(pv, n, c, hi + b * ld, lo ? lo + b * ld : nullptr);
 }
 
+// Short vectors (n <= kCgSmallMaxN): one CTA per probe runs everything of an
+// iteration after the operator product -- pAp, X += alpha P, R -= alpha W,
+// ||R||^2 and, for a probe that ran, P = R + beta P with its bf16 copies -- in
+// one launch, where longer vectors take a projection, an update and a
+// direction launch.  Each thread holds its E elements of R, P and W in
+// registers (element threadIdx.x + e * 1024), so one round of loads feeds all
+// three phases.  The per-element arithmetic is that of cg_update_kernel and
+// cg_direction_kernel.  Dot products accumulate in T within a warp and in
+// float64 over the 32 warps: this GPU's float64 rate is a small fraction of
+// its float32 rate, and one SM doing every product in float64 took longer
+// than the three launches it replaces.
+constexpr int kCgSmallThreads = 1024;
+
+template <typename T>
+__device__ __forceinline__ double cta_sum_small(T v, double *red) {
+  v = warp_sum_t<T>(v);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = (double)v;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const double t = warp_sum(red[threadIdx.x]);
+    if (threadIdx.x == 0) red[32] = t;
+  }
+  __syncthreads();
+  const double t = red[32];
+  __syncthreads();  // red is reused by the next sum
+  return t;
+}
+
+template <typename T, int E>
+__global__ void __launch_bounds__(kCgSmallThreads)
+cg_step_small_kernel(T *__restrict__ X, T *__restrict__ R, T *__restrict__ P,
+                     const T *__restrict__ W, int64_t ld, int64_t n,
+                     const double *__restrict__ rs, const double *__restrict__ thr,
+                     double *__restrict__ rs_next, int *__restrict__ nactive,
+                     int *__restrict__ nactive_clear, int *__restrict__ iters,
+                     __nv_bfloat16 *hi, __nv_bfloat16 *lo) {
+  __shared__ double red[33];
+  const int64_t b = blockIdx.x;
+  if (b == 0 && threadIdx.x == 0) *nactive_clear = 0;  // the next iteration's count
+  const double rsb = rs[b];
+  const bool active = rsb > thr[b];  // uniform over the CTA
+  T *x = X + b * ld, *r = R + b * ld, *pv = P + b * ld;
+  const T *w = W + b * ld;
+  T rv[E], pe[E], we[E];
+#pragma unroll
+  for (int e = 0; e < E; ++e) {
+    const int64_t i = threadIdx.x + (int64_t)e * kCgSmallThreads;
+    const bool in = i < n;
+    rv[e] = in ? r[i] : (T)0;
+    pe[e] = in && active ? pv[i] : (T)0;
+    we[e] = in && active ? w[i] : (T)0;
+  }
+  T rr = (T)0;
+  if (active) {
+    T acc = (T)0;
+#pragma unroll
+    for (int e = 0; e < E; ++e) acc = fma(pe[e], we[e], acc);
+    const T alpha = (T)(rsb / cta_sum_small<T>(acc, red));
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      const int64_t i = threadIdx.x + (int64_t)e * kCgSmallThreads;
+      rv[e] = fma(-alpha, we[e], rv[e]);
+      if (i < n) {
+        x[i] = fma(alpha, pe[e], x[i]);  // X is read only here
+        r[i] = rv[e];
+      }
+    }
+  }
+#pragma unroll
+  for (int e = 0; e < E; ++e) rr = fma(rv[e], rv[e], rr);
+  const double t = cta_sum_small<T>(rr, red);
+  if (threadIdx.x == 0) {
+    rs_next[b] = t;
+    if (active) {
+      if (iters) iters[b] += 1;
+      if (t > thr[b]) atomicAdd(nactive, 1);
+    }
+  }
+  if (!active) return;
+  const T beta = (T)(t / rsb);
+  __nv_bfloat16 *h = hi ? hi + b * ld : nullptr, *l = lo ? lo + b * ld : nullptr;
+#pragma unroll
+  for (int e = 0; e < E; ++e) {
+    const int64_t i = threadIdx.x + (int64_t)e * kCgSmallThreads;
+    if (i >= n) continue;
+    const T pn = fma(beta, pe[e], rv[e]);
+    pv[i] = pn;
+    if (h) {
+      const float f = (float)pn;
+      const __nv_bfloat16 hb = __float2bfloat16_rn(f);
+      h[i] = hb;
+      if (l) l[i] = __float2bfloat16_rn(f - __bfloat162float(hb));
+    }
+  }
+}
+
 template <typename T>
 int launch_cg_init(const T *B, T *X, T *R, T *P, int64_t ld, int64_t n, int64_t p,
                    __nv_bfloat16 *hi, __nv_bfloat16 *lo, double *partials, unsigned *counters,
@@ -1321,12 +1421,38 @@ int launch_cg_init(const T *B, T *X, T *R, T *P, int64_t ld, int64_t n, int64_t 
 template <typename T>
 int launch_cg_update(T *X, T *R, const T *P, const T *W, int64_t ld, int64_t n, int64_t p,
                      const double *rs, const double *pap, const double *thr, double *partials,
-                     unsigned *counters, double *rs_next, int *nactive, int *iters, cudaStream_t s) {
+                     unsigned *counters, double *rs_next, int *nactive, int *nactive_clear,
+                     int *iters, cudaStream_t s) {
   if (p <= 0 || n <= 0) return MFG_OK;
   if (p > 65535) return MFG_ERR_UNSUPPORTED;
   const int64_t nch = num_chunks<T>(n);
   cg_update_kernel<T><<<dim3((unsigned)nch, (unsigned)p), kThreads, 0, s>>>(
-      X, R, P, W, ld, n, rs, pap, thr, (int)nch, partials, counters, rs_next, nactive, iters);
+      X, R, P, W, ld, n, rs, pap, thr, (int)nch, partials, counters, rs_next, nactive,
+      nactive_clear, iters);
+  return MFG_LAUNCH_STATUS();
+}
+
+template <typename T>
+int launch_cg_step_small(T *X, T *R, T *P, const T *W, int64_t ld, int64_t n, int64_t p,
+                         const double *rs, const double *thr, double *rs_next, int *nactive,
+                         int *nactive_clear, int *iters, __nv_bfloat16 *hi, __nv_bfloat16 *lo,
+                         cudaStream_t s) {
+  if (p <= 0 || n <= 0) return MFG_OK;
+  if (n > kCgSmallMaxN || p > 0x7fffffff) return MFG_ERR_UNSUPPORTED;
+  static_assert(kCgSmallMaxN == 8 * kCgSmallThreads, "elements per thread");
+  const unsigned grid = (unsigned)p;
+  if (n <= kCgSmallThreads)
+    cg_step_small_kernel<T, 1><<<grid, kCgSmallThreads, 0, s>>>(
+        X, R, P, W, ld, n, rs, thr, rs_next, nactive, nactive_clear, iters, hi, lo);
+  else if (n <= 2 * kCgSmallThreads)
+    cg_step_small_kernel<T, 2><<<grid, kCgSmallThreads, 0, s>>>(
+        X, R, P, W, ld, n, rs, thr, rs_next, nactive, nactive_clear, iters, hi, lo);
+  else if (n <= 4 * kCgSmallThreads)
+    cg_step_small_kernel<T, 4><<<grid, kCgSmallThreads, 0, s>>>(
+        X, R, P, W, ld, n, rs, thr, rs_next, nactive, nactive_clear, iters, hi, lo);
+  else
+    cg_step_small_kernel<T, 8><<<grid, kCgSmallThreads, 0, s>>>(
+        X, R, P, W, ld, n, rs, thr, rs_next, nactive, nactive_clear, iters, hi, lo);
   return MFG_LAUNCH_STATUS();
 }
 
@@ -1615,7 +1741,10 @@ template int launch_twosweep_finish<float>(float *, int64_t, const float *, int6
                                  double, double, double *, double *, int *, cudaStream_t);    \
   template int launch_cg_update<T>(T *, T *, const T *, const T *, int64_t, int64_t, int64_t,  \
                                    const double *, const double *, const double *, double *,  \
-                                   unsigned *, double *, int *, int *, cudaStream_t);         \
+                                   unsigned *, double *, int *, int *, int *, cudaStream_t);  \
+  template int launch_cg_step_small<T>(T *, T *, T *, const T *, int64_t, int64_t, int64_t,     \
+                                       const double *, const double *, double *, int *, int *, \
+                                       int *, __nv_bfloat16 *, __nv_bfloat16 *, cudaStream_t); \
   template int launch_cg_direction<T>(T *, const T *, int64_t, int64_t, int64_t,              \
                                       const double *, const double *, const double *,         \
                                       __nv_bfloat16 *, __nv_bfloat16 *, cudaStream_t);        \

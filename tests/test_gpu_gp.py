@@ -71,6 +71,25 @@ def test_cg_tensor_core_rbf_operator(n):
     assert np.abs(sol.double().cpu().numpy() - want).max() <= 1e-4 * np.abs(want).max()
 
 
+def test_cg_long_vectors_multi_launch_iteration():
+    # n above the one-CTA-per-probe step (8192): the iteration runs as a
+    # projection, an update and a direction launch; a zero row never starts
+    import scipy.sparse as sp
+
+    n = 40000
+    L = sp.diags([-np.ones(n - 1), 2.0 * np.ones(n), -np.ones(n - 1)], [-1, 0, 1], format="csr")
+    op = mf.CSROperator.from_scipy(L, shift=1.0)
+    rng = np.random.default_rng(11)
+    B = np.stack([rng.standard_normal(n), np.zeros(n), rng.standard_normal(n)])
+    X, its = mf.linalg.cg_batched(op, _t(B, torch.float32), tol=1e-6)
+    A = L + sp.identity(n)
+    for i in (0, 2):
+        xo, ko = gp.cg(lambda v: A @ v, B[i], tol=1e-6)
+        assert abs(int(its[i]) - ko) <= 2
+        np.testing.assert_allclose(X[i].double().cpu().numpy(), xo, atol=1e-5 * np.abs(xo).max())
+    assert int(its[1]) == 0 and not X[1].any()
+
+
 def test_rbf_logpdf_value_and_gradient_fp64_vs_oracle():
     n, k, p = 256, 20, 16
     rng = np.random.default_rng(10)
