@@ -596,12 +596,12 @@ bool tcgen05_supported_shape(int64_t n, int64_t p) {
 // Few right-hand sides (p <= 8, e.g. the one CG solve of a GP log-density):
 // the product is a stream of the operator, so it runs on the CUDA cores as a
 // GEMV over all SMs instead of as 128-row tensor-core tiles (n / 128 CTAs,
-// too few to draw HBM bandwidth).  One warp per operator row, 16-byte loads
-// of A_hi / A_lo and of the bf16 panel, float sums of the same three products
-// (hi hi + hi lo + lo hi), a fixed-order warp butterfly per probe.  The
-// operator loads of the next 256 columns are issued before the current ones
-// are used (two in flight per lane) and bypass L1, which keeps the panel
-// that every warp of the SM re-reads there.
+// too few to draw HBM bandwidth).  Warps own column segments of operator
+// rows: 16-byte loads of A_hi / A_lo and of the bf16 panel, float sums of
+// the same three products (hi hi + hi lo + lo hi), a fixed-order warp
+// butterfly per probe.  The operator loads of the next 256 (one probe: 512)
+// columns are issued before the current ones are used and bypass L1, which
+// keeps the panel that every warp of the SM re-reads there.
 // ---------------------------------------------------------------------------
 
 constexpr int kGemvWarps = 8;
@@ -624,6 +624,135 @@ __device__ __forceinline__ void bf16x8_to_float(const uint4 &u, float (&f)[8]) {
   }
 }
 
+// Each row is cut into kGemvSeg column segments, one warp each, so that a
+// launch has kGemvSeg * n warp tasks: with one warp per row (n tasks against
+// ~6000 resident warps) the last partial wave ran with too few loads in
+// flight.  The segment sums are added in a fixed order.
+constexpr int kGemvSeg = 4;
+constexpr int kGemvRows = kGemvWarps / kGemvSeg;  // rows per CTA
+
+// kDeep: loads of two iterations ahead in flight instead of one (for one
+// probe, whose products are too few to cover the latency; with more probes
+// the deeper ring costs occupancy).
+template <int P, bool kSplit, bool kDeep>
+__device__ __forceinline__ void gemv_rows(const __nv_bfloat16 *__restrict__ Ahi,
+                                          const __nv_bfloat16 *__restrict__ Alo, int64_t lda,
+                                          const __nv_bfloat16 *__restrict__ Vhi,
+                                          const __nv_bfloat16 *__restrict__ Vlo, int64_t ldvb,
+                                          const float *__restrict__ Vf, int64_t ldvf,
+                                          float *__restrict__ W, int64_t ldw, int n, int p,
+                                          float shift) {
+  constexpr int kAhead = kDeep ? 512 : 256;
+  __shared__ float part[kGemvWarps][P];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int seg = warp % kGemvSeg;
+  const int64_t m = (int64_t)blockIdx.x * kGemvRows + warp / kGemvSeg;
+  float acc[P];
+#pragma unroll
+  for (int b = 0; b < P; ++b) acc[b] = 0.f;
+  if (m < n) {  // warp-uniform; every warp reaches the barrier below
+    const __nv_bfloat16 *ah = Ahi + m * lda;
+    const __nv_bfloat16 *al = kSplit ? Alo + m * lda : nullptr;
+    const int n8 = n & ~7;
+    const int seg_len = ((n8 / 8 + kGemvSeg - 1) / kGemvSeg) * 8;  // a multiple of 8 columns
+    const int c0 = seg * seg_len;
+    const int c1 = min(c0 + seg_len, n8);
+    const uint4 zero = make_uint4(0u, 0u, 0u, 0u);
+    uint4 h0 = zero, l0 = zero, h1 = zero, l1 = zero;
+    const int cl = c0 + lane * 8;
+    if (cl < c1) {
+      h0 = ld_stream16(ah + cl);
+      if (kSplit) l0 = ld_stream16(al + cl);
+    }
+    if (kDeep && cl + 256 < c1) {
+      h1 = ld_stream16(ah + cl + 256);
+      if (kSplit) l1 = ld_stream16(al + cl + 256);
+    }
+    for (int c = cl; c < c1; c += 256) {
+      uint4 h2 = zero, l2 = zero;
+      if (c + kAhead < c1) {
+        h2 = ld_stream16(ah + c + kAhead);
+        if (kSplit) l2 = ld_stream16(al + c + kAhead);
+      }
+      float a1[8], a2[8];
+      bf16x8_to_float(h0, a1);
+      if (kSplit) bf16x8_to_float(l0, a2);
+      if (kDeep) {
+        h0 = h1;
+        l0 = l1;
+        h1 = h2;
+        l1 = l2;
+      } else {
+        h0 = h2;
+        l0 = l2;
+      }
+#pragma unroll
+      for (int b = 0; b < P; ++b) {
+        if (b >= p) break;
+        float v1[8], v2[8];
+        bf16x8_to_float(__ldg(reinterpret_cast<const uint4 *>(Vhi + b * ldvb + c)), v1);
+        if (kSplit)
+          bf16x8_to_float(__ldg(reinterpret_cast<const uint4 *>(Vlo + b * ldvb + c)), v2);
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+          acc[b] = fmaf(a1[t], v1[t], acc[b]);
+          if (kSplit) {
+            acc[b] = fmaf(a1[t], v2[t], acc[b]);
+            acc[b] = fmaf(a2[t], v1[t], acc[b]);
+          }
+        }
+      }
+    }
+    if (seg == kGemvSeg - 1) {
+      for (int c = n8 + lane; c < n; c += 32) {  // columns past the last multiple of 8
+        const float x1 = __bfloat162float(ah[c]);
+        const float x2 = kSplit ? __bfloat162float(al[c]) : 0.f;
+#pragma unroll
+        for (int b = 0; b < P; ++b) {
+          if (b >= p) break;
+          const float y1 = __bfloat162float(Vhi[b * ldvb + c]);
+          acc[b] = fmaf(x1, y1, acc[b]);
+          if (kSplit) {
+            acc[b] = fmaf(x1, __bfloat162float(Vlo[b * ldvb + c]), acc[b]);
+            acc[b] = fmaf(x2, y1, acc[b]);
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int b = 0; b < P; ++b) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc[b] += __shfl_xor_sync(0xffffffffu, acc[b], o);
+    }
+  }
+  if (lane == 0) {
+#pragma unroll
+    for (int b = 0; b < P; ++b) part[warp][b] = acc[b];
+  }
+  __syncthreads();
+  if (threadIdx.x < kGemvRows * P) {
+    const int r = threadIdx.x / P, b = threadIdx.x % P;
+    const int64_t row = (int64_t)blockIdx.x * kGemvRows + r;
+    if (row < n && b < p) {
+      float t = 0.f;
+#pragma unroll
+      for (int q = 0; q < kGemvSeg; ++q) t += part[r * kGemvSeg + q][b];
+      W[b * ldw + row] = fmaf(shift, __ldg(Vf + b * ldvf + row), t);
+    }
+  }
+}
+
+// one probe: 48 registers keep five CTAs on an SM with the deeper ring
+template <bool kSplit>
+__global__ void __launch_bounds__(32 * kGemvWarps, 5)
+dense_gemv1_kernel(const __nv_bfloat16 *__restrict__ Ahi, const __nv_bfloat16 *__restrict__ Alo,
+                   int64_t lda, const __nv_bfloat16 *__restrict__ Vhi,
+                   const __nv_bfloat16 *__restrict__ Vlo, int64_t ldvb,
+                   const float *__restrict__ Vf, int64_t ldvf, float *__restrict__ W, int64_t ldw,
+                   int n, int p, float shift) {
+  gemv_rows<1, kSplit, true>(Ahi, Alo, lda, Vhi, Vlo, ldvb, Vf, ldvf, W, ldw, n, p, shift);
+}
+
 template <int P, bool kSplit>
 __global__ void __launch_bounds__(32 * kGemvWarps)
 dense_gemv_kernel(const __nv_bfloat16 *__restrict__ Ahi, const __nv_bfloat16 *__restrict__ Alo,
@@ -631,71 +760,7 @@ dense_gemv_kernel(const __nv_bfloat16 *__restrict__ Ahi, const __nv_bfloat16 *__
                   const __nv_bfloat16 *__restrict__ Vlo, int64_t ldvb,
                   const float *__restrict__ Vf, int64_t ldvf, float *__restrict__ W, int64_t ldw,
                   int n, int p, float shift) {
-  const int lane = threadIdx.x & 31;
-  const int64_t m = (int64_t)blockIdx.x * kGemvWarps + (threadIdx.x >> 5);
-  if (m >= n) return;  // warp-uniform
-  const __nv_bfloat16 *ah = Ahi + m * lda;
-  const __nv_bfloat16 *al = kSplit ? Alo + m * lda : nullptr;
-  float acc[P];
-#pragma unroll
-  for (int b = 0; b < P; ++b) acc[b] = 0.f;
-  const int n8 = n & ~7;
-  uint4 hcur = make_uint4(0u, 0u, 0u, 0u), lcur = hcur;
-  if (lane * 8 < n8) {
-    hcur = ld_stream16(ah + lane * 8);
-    if (kSplit) lcur = ld_stream16(al + lane * 8);
-  }
-  for (int c = lane * 8; c < n8; c += 256) {
-    uint4 hnext = make_uint4(0u, 0u, 0u, 0u), lnext = hnext;
-    if (c + 256 < n8) {
-      hnext = ld_stream16(ah + c + 256);
-      if (kSplit) lnext = ld_stream16(al + c + 256);
-    }
-    float a1[8], a2[8];
-    bf16x8_to_float(hcur, a1);
-    if (kSplit) bf16x8_to_float(lcur, a2);
-    hcur = hnext;
-    lcur = lnext;
-#pragma unroll
-    for (int b = 0; b < P; ++b) {
-      if (b >= p) break;
-      float v1[8], v2[8];
-      bf16x8_to_float(__ldg(reinterpret_cast<const uint4 *>(Vhi + b * ldvb + c)), v1);
-      if (kSplit) bf16x8_to_float(__ldg(reinterpret_cast<const uint4 *>(Vlo + b * ldvb + c)), v2);
-#pragma unroll
-      for (int t = 0; t < 8; ++t) {
-        acc[b] = fmaf(a1[t], v1[t], acc[b]);
-        if (kSplit) {
-          acc[b] = fmaf(a1[t], v2[t], acc[b]);
-          acc[b] = fmaf(a2[t], v1[t], acc[b]);
-        }
-      }
-    }
-  }
-  for (int c = n8 + lane; c < n; c += 32) {  // columns past the last multiple of 8
-    const float x1 = __bfloat162float(ah[c]);
-    const float x2 = kSplit ? __bfloat162float(al[c]) : 0.f;
-#pragma unroll
-    for (int b = 0; b < P; ++b) {
-      if (b >= p) break;
-      const float y1 = __bfloat162float(Vhi[b * ldvb + c]);
-      acc[b] = fmaf(x1, y1, acc[b]);
-      if (kSplit) {
-        acc[b] = fmaf(x1, __bfloat162float(Vlo[b * ldvb + c]), acc[b]);
-        acc[b] = fmaf(x2, y1, acc[b]);
-      }
-    }
-  }
-#pragma unroll
-  for (int b = 0; b < P; ++b) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc[b] += __shfl_xor_sync(0xffffffffu, acc[b], o);
-  }
-  if (lane == 0) {
-#pragma unroll
-    for (int b = 0; b < P; ++b)
-      if (b < p) W[b * ldw + m] = fmaf(shift, __ldg(Vf + b * ldvf + m), acc[b]);
-  }
+  gemv_rows<P, kSplit, false>(Ahi, Alo, lda, Vhi, Vlo, ldvb, Vf, ldvf, W, ldw, n, p, shift);
 }
 
 template <int P>
@@ -703,13 +768,22 @@ static void launch_gemv_p(bool split, const __nv_bfloat16 *A_hi, const __nv_bflo
                           int64_t lda, const __nv_bfloat16 *V_hi, const __nv_bfloat16 *V_lo,
                           int64_t ldvb, const float *Vf, int64_t ldvf, float *W, int64_t ldw,
                           int n, int p, float shift, cudaStream_t s) {
-  const unsigned grid = (unsigned)((n + kGemvWarps - 1) / kGemvWarps);
-  if (split)
-    dense_gemv_kernel<P, true><<<grid, 32 * kGemvWarps, 0, s>>>(A_hi, A_lo, lda, V_hi, V_lo, ldvb,
+  const unsigned grid = (unsigned)((n + kGemvRows - 1) / kGemvRows);
+  if constexpr (P == 1) {
+    if (split)
+      dense_gemv1_kernel<true><<<grid, 32 * kGemvWarps, 0, s>>>(A_hi, A_lo, lda, V_hi, V_lo, ldvb,
                                                                 Vf, ldvf, W, ldw, n, p, shift);
-  else
-    dense_gemv_kernel<P, false><<<grid, 32 * kGemvWarps, 0, s>>>(A_hi, A_lo, lda, V_hi, V_lo, ldvb,
-                                                                 Vf, ldvf, W, ldw, n, p, shift);
+    else
+      dense_gemv1_kernel<false><<<grid, 32 * kGemvWarps, 0, s>>>(A_hi, A_lo, lda, V_hi, V_lo,
+                                                                 ldvb, Vf, ldvf, W, ldw, n, p, shift);
+  } else {
+    if (split)
+      dense_gemv_kernel<P, true><<<grid, 32 * kGemvWarps, 0, s>>>(A_hi, A_lo, lda, V_hi, V_lo,
+                                                                  ldvb, Vf, ldvf, W, ldw, n, p, shift);
+    else
+      dense_gemv_kernel<P, false><<<grid, 32 * kGemvWarps, 0, s>>>(A_hi, A_lo, lda, V_hi, V_lo,
+                                                                   ldvb, Vf, ldvf, W, ldw, n, p, shift);
+  }
 }
 
 constexpr int64_t kGemvMaxP = 8;

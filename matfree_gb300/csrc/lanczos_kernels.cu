@@ -1258,7 +1258,10 @@ cg_update_kernel(T *__restrict__ X, T *__restrict__ R, const T *__restrict__ P,
   T r[kVPT][VW];
   load_chunk<T, false>(R + b * ld, n, c, r);
   if (active) {
-    const T alpha = (T)(rs[b] / pap[b]);
+    __shared__ T alpha_s;  // one float64 division per CTA, not per thread
+    if (threadIdx.x == 0) alpha_s = (T)(rs[b] / pap[b]);
+    __syncthreads();
+    const T alpha = alpha_s;
     T x[kVPT][VW], pv[kVPT][VW], wv[kVPT][VW];
     load_chunk<T, false>(X + b * ld, n, c, x);
     load_chunk<T>(P + b * ld, n, c, pv);
@@ -1298,7 +1301,10 @@ cg_direction_kernel(T *__restrict__ P, const T *__restrict__ R, int64_t ld, int6
   constexpr int VW = Vec<T>::width;
   const int64_t c = blockIdx.x, b = blockIdx.y;
   if (!(rs[b] > thr[b])) return;
-  const T beta = (T)(rs_next[b] / rs[b]);
+  __shared__ T beta_s;  // one float64 division per CTA, not per thread
+  if (threadIdx.x == 0) beta_s = (T)(rs_next[b] / rs[b]);
+  __syncthreads();
+  const T beta = beta_s;
   T pv[kVPT][VW], r[kVPT][VW];
   load_chunk<T, false>(P + b * ld, n, c, pv);
   load_chunk<T>(R + b * ld, n, c, r);
@@ -1347,30 +1353,38 @@ cg_step_small_kernel(T *__restrict__ X, T *__restrict__ R, T *__restrict__ P,
                      int *__restrict__ nactive_clear, int *__restrict__ iters,
                      __nv_bfloat16 *hi, __nv_bfloat16 *lo) {
   __shared__ double red[33];
+  __shared__ T coef;  // alpha, then beta: one float64 division each, in thread 0
+  __shared__ int run;
   const int64_t b = blockIdx.x;
-  if (b == 0 && threadIdx.x == 0) *nactive_clear = 0;  // the next iteration's count
-  const double rsb = rs[b];
-  const bool active = rsb > thr[b];  // uniform over the CTA
   T *x = X + b * ld, *r = R + b * ld, *pv = P + b * ld;
   const T *w = W + b * ld;
   T rv[E], pe[E], we[E];
 #pragma unroll
-  for (int e = 0; e < E; ++e) {
-    const int64_t i = threadIdx.x + (int64_t)e * kCgSmallThreads;
+  for (int e = 0; e < E; ++e) {  // issued before the barrier below
+    const int i = (int)threadIdx.x + e * kCgSmallThreads;  // n <= kCgSmallMaxN
     const bool in = i < n;
     rv[e] = in ? r[i] : (T)0;
-    pe[e] = in && active ? pv[i] : (T)0;
-    we[e] = in && active ? w[i] : (T)0;
+    pe[e] = in ? pv[i] : (T)0;
+    we[e] = in ? w[i] : (T)0;
   }
+  if (threadIdx.x == 0) {
+    if (b == 0) *nactive_clear = 0;  // the next iteration's count
+    run = rs[b] > thr[b];
+  }
+  __syncthreads();
+  const bool active = run != 0;  // uniform over the CTA
   T rr = (T)0;
   if (active) {
     T acc = (T)0;
 #pragma unroll
     for (int e = 0; e < E; ++e) acc = fma(pe[e], we[e], acc);
-    const T alpha = (T)(rsb / cta_sum_small<T>(acc, red));
+    const double pap = cta_sum_small<T>(acc, red);
+    if (threadIdx.x == 0) coef = (T)(rs[b] / pap);
+    __syncthreads();
+    const T alpha = coef;
 #pragma unroll
     for (int e = 0; e < E; ++e) {
-      const int64_t i = threadIdx.x + (int64_t)e * kCgSmallThreads;
+      const int i = (int)threadIdx.x + e * kCgSmallThreads;  // n <= kCgSmallMaxN
       rv[e] = fma(-alpha, we[e], rv[e]);
       if (i < n) {
         x[i] = fma(alpha, pe[e], x[i]);  // X is read only here
@@ -1380,20 +1394,22 @@ cg_step_small_kernel(T *__restrict__ X, T *__restrict__ R, T *__restrict__ P,
   }
 #pragma unroll
   for (int e = 0; e < E; ++e) rr = fma(rv[e], rv[e], rr);
-  const double t = cta_sum_small<T>(rr, red);
+  const double t = cta_sum_small<T>(rr, red);  // every thread has read alpha by now
   if (threadIdx.x == 0) {
     rs_next[b] = t;
     if (active) {
       if (iters) iters[b] += 1;
       if (t > thr[b]) atomicAdd(nactive, 1);
+      coef = (T)(t / rs[b]);
     }
   }
   if (!active) return;
-  const T beta = (T)(t / rsb);
+  __syncthreads();
+  const T beta = coef;
   __nv_bfloat16 *h = hi ? hi + b * ld : nullptr, *l = lo ? lo + b * ld : nullptr;
 #pragma unroll
   for (int e = 0; e < E; ++e) {
-    const int64_t i = threadIdx.x + (int64_t)e * kCgSmallThreads;
+    const int i = (int)threadIdx.x + e * kCgSmallThreads;  // n <= kCgSmallMaxN
     if (i >= n) continue;
     const T pn = fma(beta, pe[e], rv[e]);
     pv[i] = pn;
