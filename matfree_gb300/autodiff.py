@@ -16,6 +16,10 @@ The reverse pass mirrors what JAX differentiates in matfree:
 
 Step 1 runs as batched torch linear algebra on the GPU on p small k x k
 matrices; everything of size n runs in the CUDA library.
+
+``rbf_logdet`` does step 4 for the RBF kernel's three log-parameters;
+``callback_quadform`` does it for any callable matvec(v, *params) with one
+autograd VJP of the callable over the stacked basis.
 """
 
 from __future__ import annotations
@@ -28,7 +32,8 @@ import torch
 from . import _lib
 from ._panel import Workspace, as_panel, padded_ld, require_cuda, stream_ptr
 from .decomp import run_hessenberg, two_sweep_applies
-from .operators import DenseOperator, RBFKernelOperator
+from .operators import CallbackOperator, DenseOperator, RBFKernelOperator
+from .tree import _rebuild, tree_leaves
 
 _WS = Workspace()
 
@@ -140,6 +145,10 @@ def _forward_panels(op, k, panel, ld):
                                 ctypes.c_void_p(Q.data_ptr()), ctypes.c_void_p(H.data_ptr()),
                                 ctypes.c_void_p(R.data_ptr()), ctypes.c_void_p(c.data_ptr()), ws,
                                 wsb, stream_ptr())
+        err = getattr(op, "error", None)
+        if err is not None:  # a callback operator raised inside the Krylov loop
+            op.error = None
+            raise err
         _lib.check(st, "mfg_hessenberg")
         if mode == 1:
             break
@@ -197,5 +206,99 @@ def rbf_logdet(x: torch.Tensor, theta: torch.Tensor, probes: torch.Tensor, num_m
     return _RBFLogdet.apply(theta, x.to(torch.float32).contiguous(), probes, int(num_matvecs), precision)
 
 
+def _fun_pair(dense_funm):
+    """(f, f') on float64 eigenvalue tensors for an integrand's matrix function.
+
+    log, exp(a x) and x**a have closed-form derivatives; any other elementwise
+    torch callable is differentiated with torch autograd.
+    """
+    kind, a = dense_funm.kind, dense_funm.param
+    if kind == _lib.MFG_FUN_LOG:
+        return torch.log, lambda x: 1.0 / x
+    if kind == _lib.MFG_FUN_EXP:
+        return (lambda x: torch.exp(a * x)), (lambda x: a * torch.exp(a * x))
+    if kind == _lib.MFG_FUN_POW:
+        return (lambda x: x ** a), (lambda x: a * x ** (a - 1.0))
+    f = dense_funm.apply_scalar
+
+    def fprime(x):
+        with torch.enable_grad():
+            xr = x.detach().requires_grad_(True)
+            (g,) = torch.autograd.grad(f(xr).sum(), xr)
+        return g
+
+    return f, fprime
+
+
+def params_require_grad(params) -> bool:
+    """Whether autograd should see the matvec's parameters."""
+    return torch.is_grad_enabled() and any(
+        isinstance(t, torch.Tensor) and t.requires_grad for t in tree_leaves(params))
+
+
+class _CallbackQuadform(torch.autograd.Function):
+    """Values ||v_b||^2 e1^T f(T_b) e1 of a callable matvec(v, *params), with
+    the gradient in the tensor leaves of params.
+
+    This is the SLQ integrand (matfree/funm.py:226-241) behind the custom VJP
+    of the decomposition (decomp.py:420-422, 480-600).  The forward pass keeps
+    the Krylov panels; the backward pass forms dH from the eigenvectors of T
+    (``quadform_dH``), runs the Hessenberg adjoint on the GPU for Lambda
+    (``mfg_hessenberg_adjoint``) and contracts
+    sum_{b,j} lambda_bj^T d(A(params) q_bj)/d params with one batched autograd
+    VJP of the matvec over all p*k basis vectors (the reference takes the same
+    VJP one step at a time, decomp.py:587-589).  dQ = dr = 0 (the integrand
+    reads only T), and the probes get no gradient.
+    """
+
+    @staticmethod
+    def forward(ctx, spec, samples, *leaves):
+        fn, n, k, f, fprime, batched, params_tree = spec
+        params = _rebuild(params_tree, iter(leaves))
+        op = CallbackOperator(fn, n, dtype=samples.dtype, batched=batched, params=params)
+        panel, ld = as_panel(samples, n, op.basis_dtype)
+        Q, H, R, c = _forward_panels(op, k, panel, ld)
+        values, dH = quadform_dH(H, 1.0 / (c * c), f, fprime)
+        ctx.save_for_backward(Q, H, R, c, dH)
+        ctx.spec = spec
+        ctx.op = op
+        ctx.leaves = leaves
+        return values
+
+    @staticmethod
+    def backward(ctx, gvals):
+        Q, H, R, c, dH = ctx.saved_tensors
+        fn, n, k, _f, _fp, batched, params_tree = ctx.spec
+        leaves = ctx.leaves
+        want = [i for i in range(len(leaves)) if ctx.needs_input_grad[2 + i]]
+        grads = [None] * len(leaves)
+        if want:
+            Lam, _dv = hessenberg_adjoint(ctx.op, Q, H, R, c, dH * gvals.to(dH.dtype)[:, None, None])
+            p = Q.shape[0]
+            Qf = Q[:, :, :n].reshape(p * k, n)
+            Lf = Lam[:, :, :n].reshape(p * k, n)
+            with torch.enable_grad():
+                live = [t.detach().requires_grad_(True) if i in want else t for i, t in enumerate(leaves)]
+                params = _rebuild(params_tree, iter(live))
+                AQ = CallbackOperator(fn, n, dtype=Q.dtype, batched=batched, params=params)._apply_rows(Qf)
+                total = (Lf.to(AQ.dtype) * AQ).sum()
+                gs = torch.autograd.grad(total, [live[i] for i in want], allow_unused=True)
+            for i, g in zip(want, gs):
+                grads[i] = torch.zeros_like(leaves[i]) if g is None else g.to(leaves[i].dtype)
+        return (None, None, *grads)
+
+
+def callback_quadform(fn, n: int, k: int, samples: torch.Tensor, dense_funm, params=(),
+                      batched: bool = False) -> torch.Tensor:
+    """Differentiable integrand values (p,) float64 for a callable matvec
+    ``fn(v, *params)`` (or ``fn(V, *params)`` on (p, n) panels if ``batched``)."""
+    if k <= 0:
+        # decomp.py:483-486
+        raise ValueError("Custom Hessenberg-adjoints are not implemented for num_matvecs = 0.")
+    f, fprime = _fun_pair(dense_funm)
+    spec = (fn, int(n), int(k), f, fprime, batched, tuple(params))
+    return _CallbackQuadform.apply(spec, samples, *tree_leaves(tuple(params)))
+
+
 __all__ = ["quadform_dH", "hessenberg_adjoint", "rbf_logdet", "rbf_theta_contractions",
-           "run_hessenberg"]
+           "run_hessenberg", "callback_quadform", "params_require_grad"]

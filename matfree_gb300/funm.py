@@ -21,7 +21,7 @@ import torch
 from . import _lib
 from ._panel import Workspace, as_panel, require_cuda, stream_ptr
 from .decomp import _flat_operator, _TridiagSymFull, full_reortho, run_hessenberg, two_sweep_applies
-from .operators import Operator, as_operator
+from .operators import CallbackOperator, Operator, as_operator
 from .tree import ravel_pytree
 
 _LOGS = {np.log, math.log, torch.log}
@@ -111,6 +111,14 @@ class MonteCarloFunmSym:
             from .decomp import _error_num_matvecs
 
             raise ValueError(_error_num_matvecs(k, maxval=n, minval=0))
+        if k > 0 and isinstance(op, CallbackOperator):
+            from .autodiff import callback_quadform, params_require_grad
+
+            if params_require_grad(op.params):
+                # differentiable in the matvec's parameters (the custom VJP
+                # of tridiag_sym, decomp.py:420-422)
+                return callback_quadform(op.fn, n, k, samples, self.dense_funm, op.params,
+                                         batched=op.batched)
         if self.dense_funm.kind is not None:
             return slq_values(op, k, samples, self.dense_funm.kind, self.dense_funm.param)
         # arbitrary f: device Krylov + device eigensolve, f evaluated by torch on the GPU
