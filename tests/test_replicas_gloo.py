@@ -30,7 +30,7 @@ def _worker(rank, world_size, port, out):
 @pytest.mark.timeout(120)
 def test_two_rank_replica_throughput_is_total_units_over_slowest_rank():
     port = 29500 + (os.getpid() % 1000)
-    manager = mp.Manager()
+    manager = mp.get_context("spawn").Manager()  # no fork of this multi-threaded process
     out = manager.dict()
     mp.spawn(_worker, args=(2, port, out), nprocs=2, join=True)
     for rank in (0, 1):
