@@ -1,0 +1,39 @@
+"""The reference arm of bench.py (the float64 restatement timed on the host
+cores) keeps the one-JSON-line contract, here on the small dense config.  No GPU."""
+
+import json
+import os
+import subprocess
+import sys
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _run(extra_env=None):
+    env = dict(os.environ, **(extra_env or {}))
+    return subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--config", "dense1k",
+                           "--steps", "1", "--warmup", "3"],
+                          cwd=ROOT, env=env, capture_output=True, text=True, timeout=300)
+
+
+def test_reference_arm_prints_one_contract_line():
+    out = _run()
+    assert out.returncode == 0, out.stderr
+    lines = [ln for ln in out.stdout.splitlines() if ln.strip()]
+    assert len(lines) == 1
+    line = json.loads(lines[0])
+    assert line["impl"] == "reference"
+    assert line["metric"] == "logdet solves/s" and line["unit"] == "solves/s"
+    assert line["higher_is_better"] is True and line["value"] > 0
+    assert line["steps"] == 1 and line["warmup"] >= 3
+    assert "workload" in line["config"]
+    cb = line["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == line["value"]
+    assert line["e2e"] == {"value": line["value"], "unit": "solves/s", "h2d_bytes_per_step": 0,
+                           "d2h_bytes_per_step": 0}
+
+
+def test_reference_arm_other_ranks_exit_quietly():
+    out = _run({"RANK": "1"})
+    assert out.returncode == 0, out.stderr
+    assert out.stdout.strip() == ""
