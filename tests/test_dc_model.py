@@ -6,6 +6,11 @@ It checks the algorithm the kernel implements on the CPU: eigenvalues to
 1e-12 of the spectral radius and Gauss quadratures sum_i g(lambda_i) s_1i^2 to
 1e-12 on Gaussian, Wilkinson, glued, split, tiny-coupling and zero
 tridiagonals.
+
+``dc_full`` runs the same merges carrying whole eigenvector columns instead of
+their first and last rows (the form that would replace the implicit-QL
+eigenvector kernel of the gradient's Daleckii-Krein term): S^T S = I and
+S diag(lambda) S^T = T to 1e-12 k on the same spectra.
 """
 
 import math
@@ -204,3 +209,81 @@ def test_dc_model_matches_eigh(kind, k):
     np.testing.assert_allclose(lam, w0, rtol=0, atol=1e-12 * scale)
     for g in (lambda x: np.exp(-x / scale), lambda x: np.sin(3 * x / scale)):
         assert abs(np.sum(g(lam) * fsq) - np.sum(g(w0) * S0[0] ** 2)) <= 1e-12
+
+
+def dc_full(d, e):
+    """Eigenvalues (ascending) and eigenvectors (columns) by the same merges."""
+    k = len(d)
+    LAM = np.array([d[i] - (e[i - 1] if i > 0 else 0.0) - (e[i] if i + 1 < k else 0.0) for i in range(k)])
+    S = np.eye(k)  # columns: eigenvectors of the current block-diagonal problem
+    ok = True
+    w = 1
+    while w < k:
+        for a in range(0, k - w, 2 * w):
+            mid, hi = a + w, min(a + 2 * w, k)
+            rho = e[mid - 1]
+            sg = -1.0 if rho < 0 else 1.0
+            rho = abs(rho)
+            tol = 8.0 * EPS * max(abs(LAM[a]), abs(LAM[mid - 1]), abs(LAM[mid]), abs(LAM[hi - 1]), 2.0 * rho)
+            # z: the last row of the upper block's vectors, the first row of the lower block's
+            cols = [(sg * LAM[i], S[mid - 1, i], S[a:hi, i].copy()) for i in range(a, mid)]
+            cols += [(sg * LAM[i], S[mid, i], S[a:hi, i].copy()) for i in range(mid, hi)]
+            cols.sort(key=lambda t: t[0])
+            D, Z, V, dfl = [], [], [], []
+            zs = 0.0
+            for dv, z, v in cols:
+                if rho * abs(z) <= tol:
+                    dfl.append((dv, v))
+                    continue
+                zs += z * z
+                if D and dv - D[-1] <= tol:  # close poles: the same rotation, on whole columns
+                    r = math.hypot(Z[-1], z)
+                    c, s = z / r, Z[-1] / r
+                    dfl.append((D[-1], c * V[-1] - s * v))
+                    D[-1], Z[-1], V[-1] = dv, r, s * V[-1] + c * v
+                else:
+                    D.append(dv), Z.append(z), V.append(v)
+            mk = len(D)
+            out = []
+            if mk:
+                upper = D[-1] + rho * zs * (1.0 + 16.0 * EPS) + 16.0 * EPS * abs(D[-1])
+                ZZ = [z * z for z in Z]
+                roots = []
+                for j in range(mk):
+                    x, o, conv = _secular(D, ZZ, mk, j, rho, upper)
+                    ok &= conv
+                    roots.append((x, o))
+                zh = []
+                for i in range(mk):  # Loewner
+                    prod = ((D[roots[mk - 1][1]] - D[i]) + roots[mk - 1][0]) / rho
+                    for j in range(mk - 1):
+                        prod *= ((D[roots[j][1]] - D[i]) + roots[j][0]) / (D[j if j < i else j + 1] - D[i])
+                    zh.append(math.copysign(math.sqrt(max(prod, 0.0)), Z[i]))
+                Vm = np.stack(V, axis=1)
+                for j in range(mk):
+                    x, o = roots[j]
+                    u = np.array([zh[i] / ((D[i] - D[o]) - x) for i in range(mk)])
+                    out.append((D[o] + x, Vm @ (u / np.linalg.norm(u))))
+            merged = sorted(out + dfl, key=lambda t: t[0])
+            if sg < 0:
+                merged = [(-v, vec) for v, vec in reversed(merged)]
+            for t, (v, vec) in enumerate(merged):
+                LAM[a + t] = v
+                S[:, a + t] = 0.0
+                S[a:hi, a + t] = vec
+        w *= 2
+    return LAM, S, ok
+
+
+@pytest.mark.parametrize("kind", ["normal", "wilkinson", "glued", "split", "tiny", "negative", "zero"])
+@pytest.mark.parametrize("k", [1, 2, 17, 48, 100])
+def test_dc_full_vectors_match_eigh(kind, k):
+    rng = np.random.default_rng(100 * sum(map(ord, kind)) + k)
+    d, e = _case(kind, k, rng) if k > 1 else (rng.standard_normal(1), np.zeros(0))
+    T = np.diag(d) + np.diag(e, 1) + np.diag(e, -1)
+    lam, S, ok = dc_full(d, e)
+    assert ok
+    scale = max(np.abs(np.linalg.eigvalsh(T)).max(), 1e-300)
+    np.testing.assert_allclose(lam, np.linalg.eigvalsh(T), rtol=0, atol=1e-12 * scale)
+    np.testing.assert_allclose(S.T @ S, np.eye(k), atol=1e-12 * k)
+    np.testing.assert_allclose((S * lam) @ S.T, T, atol=1e-12 * k * scale)
