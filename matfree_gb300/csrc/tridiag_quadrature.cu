@@ -295,9 +295,8 @@ __global__ void tridiag_eigh_full_kernel(int k, int64_t p, const double *__restr
   if (!ok && lane == 0 && status) atomicExch(status, (int)MFG_ERR_NO_CONVERGENCE);
 }
 
-int launch_tridiag_eigh_full(int64_t k, int64_t p, const double *H, double *w, double *S,
-                             double *Z, int *status, cudaStream_t s) {
-  if (p <= 0 || k <= 0) return MFG_OK;
+static int launch_tridiag_eigh_ql(int64_t k, int64_t p, const double *H, double *w, double *S,
+                                  double *Z, int *status, cudaStream_t s) {
   const size_t smem = (size_t)4 * k * sizeof(double) + (size_t)k * sizeof(int);
   if (smem > 48 * 1024) return MFG_ERR_UNSUPPORTED;
   tridiag_eigh_full_kernel<<<(unsigned)p, 32, smem, s>>>((int)k, p, H, w, S, Z, status);
@@ -531,8 +530,11 @@ constexpr int kDcNarrow = 16;       // merges up to this size: one lane per root
 
 // Phases B-D of one level (merges of width 2^(s+1)): the secular roots, the
 // Loewner zhat and the new first/last rows, one group of G lanes per root.
-template <int G>
-__device__ bool dc_merge_roots(const DcArrays &Ar, int k, int s, int nm) {
+// kVec: instead of new first/last rows, the normalised coefficients u of
+// each root's vector in the kept poles' columns, U[r * k + i] (r the root's
+// index in the problem, i < mk).
+template <int G, bool kVec = false>
+__device__ bool dc_merge_roots(const DcArrays &Ar, int k, int s, int nm, double *U = nullptr) {
   double *D = Ar.D, *Z = Ar.Z, *F = Ar.F, *L = Ar.L, *X = Ar.X, *NF = Ar.NF, *NL = Ar.NL;
   const double *RH = Ar.RH, *UB = Ar.UB;
   int *O = Ar.O;
@@ -591,16 +593,25 @@ __device__ bool dc_merge_roots(const DcArrays &Ar, int k, int s, int nm) {
     for (int i = sub; i < mk; i += G) {
       const double u = Z[a + i] * rcp_nr((P[i] - ox) - x);
       s2 = fma(u, u, s2);
-      sf = fma(F[a + i], u, sf);
-      sl = fma(L[a + i], u, sl);
+      if (!kVec) {
+        sf = fma(F[a + i], u, sf);
+        sl = fma(L[a + i], u, sl);
+      }
     }
-    s2 = group_sum<G>(s2, gm);
-    sf = group_sum<G>(sf, gm);
-    sl = group_sum<G>(sl, gm);
+    s2 = group_sum<G>(s2, gm);  // in every lane of the group
+    const double rn = rsqrt(s2);
+    if (kVec) {
+      for (int i = sub; i < mk; i += G)
+        U[(size_t)r * k + i] = Z[a + i] * rcp_nr((P[i] - ox) - x) * rn;
+    } else {
+      sf = group_sum<G>(sf, gm);
+      sl = group_sum<G>(sl, gm);
+    }
     if (sub == 0) {
-      const double rn = rsqrt(s2);
-      NF[r] = sf * rn;
-      NL[r] = sl * rn;
+      if (!kVec) {
+        NF[r] = sf * rn;
+        NL[r] = sl * rn;
+      }
       X[r] = ox + x;
     }
   }
@@ -813,6 +824,231 @@ __global__ void __launch_bounds__(kDcMaxThreads, 1)
   }
 }
 
+// ---------------------------------------- divide and conquer with eigenvectors
+//
+// The levels, deflation, secular roots and Loewner vectors of
+// tridiag_dc_kernel, carrying every eigenvector column (rows a..hi-1 of its
+// merge; zero elsewhere) in shared memory instead of first and last rows.
+// S, S2 and U are k x k, column c of S at S[c * k].
+//   A (one thread per merge): sorted merge of the halves with deflation; each
+//     pole keeps the index CI of its column in S (z is that column's entry in
+//     row mid-1 or mid), and a close-pole rotation combines two columns in
+//     place;
+//   B, C, D: dc_merge_roots<G, true>, which leaves each root's normalised
+//     coefficients in U;
+//   D' (all threads over (column, row) pairs): S2[:, a+j] = S[:, CI[a..a+mk)]
+//     U[a+j, :] for the roots, and S2[:, c] = S[:, CI[c]] for the deflated
+//     poles c >= a+mk;
+//   E: the order of the merged eigenvalues as a column map (in O), then S
+//     from S2 through that map.
+// A direct restatement runs on the CPU as dc_full in the tests.
+constexpr int kDcvMaxK = 64;  // S, S2, U: 3 k^2 doubles (96 KB at k = 64)
+
+__host__ inline size_t dcv_smem_bytes(int k) {
+  return (dc_layout(k).words + (size_t)3 * k * k + ((size_t)k + 1) / 2) * sizeof(double);
+}
+
+__global__ void __launch_bounds__(kDcMaxThreads, 1)
+    tridiag_dcv_kernel(int k, int64_t p, const double *__restrict__ H, double *__restrict__ w_out,
+                       double *__restrict__ S_out, int *__restrict__ status) {
+  extern __shared__ double sm[];
+  const int tid = threadIdx.x;
+  const int nt = blockDim.x;
+  const int64_t b = blockIdx.x;
+  const DcLayout Ly = dc_layout(k);
+  double *LAM = sm;
+  double *FR = LAM + k;  // unused here (same layout as tridiag_dc_kernel)
+  double *LR = FR + k;
+  double *D = LR + k;
+  double *Z = D + k;
+  double *F = Z + k;
+  double *L = F + k;
+  double *X = L + k;
+  double *NF = X + k;
+  double *NL = NF + k;
+  double *EO = NL + k;
+  double *RH = EO + k;
+  double *UB = RH + Ly.kh;
+  int *O = reinterpret_cast<int *>(UB + Ly.kh);
+  int *MS = O + k;
+  double *S = sm + Ly.words;
+  double *S2 = S + (size_t)k * k;
+  double *U = S2 + (size_t)k * k;
+  int *CI = reinterpret_cast<int *>(U + (size_t)k * k);
+  const DcArrays Ar{D, Z, F, L, X, NF, NL, RH, UB, O, MS};
+
+  const double *Hb = H + (size_t)b * k * k;
+  for (int i = tid; i < k; i += nt)
+    EO[i] = (i + 1 < k) ? 0.5 * (Hb[(size_t)i * k + i + 1] + Hb[(size_t)(i + 1) * k + i]) : 0.0;
+  __syncthreads();
+  for (int i = tid; i < k; i += nt) LAM[i] = Hb[(size_t)i * k + i] - (i > 0 ? EO[i - 1] : 0.0) - EO[i];
+  for (int idx = tid; idx < k * k; idx += nt) S[idx] = (idx / k == idx % k) ? 1.0 : 0.0;
+  __syncthreads();
+  bool ok = true;
+  for (int s = 0; (1 << s) < k; ++s) {
+    const int w = 1 << s;
+    const int span = 2 * w;
+    const int nm = (k - w - 1) / span + 1;
+    // A
+    for (int q = tid; q < nm; q += nt) {
+      const int a = q * span, mid = a + w, hi = min(a + span, k);
+      double rho = EO[mid - 1];
+      const bool flip = rho < 0.0;
+      const double sg = flip ? -1.0 : 1.0;
+      rho = fabs(rho);
+      const double maxabs = fmax(fmax(fabs(LAM[a]), fabs(LAM[mid - 1])),
+                                 fmax(fabs(LAM[mid]), fabs(LAM[hi - 1])));
+      const double tol = 8.0 * DBL_EPSILON * fmax(maxabs, 2.0 * rho);
+      const int n1 = mid - a, n2 = hi - mid;
+      int c1 = 0, c2 = 0, kp = a, dp = hi;
+      double zs = 0.0;
+      for (int t = a; t < hi; ++t) {
+        bool take1;
+        if (c1 == n1)
+          take1 = false;
+        else if (c2 == n2)
+          take1 = true;
+        else
+          take1 = sg * LAM[flip ? mid - 1 - c1 : a + c1] <= sg * LAM[flip ? hi - 1 - c2 : mid + c2];
+        double d, z;
+        int col;
+        if (take1) {
+          col = flip ? mid - 1 - c1 : a + c1;
+          z = S[(size_t)col * k + (mid - 1)];  // last row of the upper block
+          ++c1;
+        } else {
+          col = flip ? hi - 1 - c2 : mid + c2;
+          z = S[(size_t)col * k + mid];  // first row of the lower block
+          ++c2;
+        }
+        d = sg * LAM[col];
+        if (rho * fabs(z) <= tol) {
+          --dp;
+          D[dp] = d;
+          CI[dp] = col;
+          continue;
+        }
+        zs = fma(z, z, zs);
+        if (kp > a && d - D[kp - 1] <= tol) {
+          // close poles: the dropped column is c Vprev - sn Vcur (in column
+          // cp), the kept one sn Vprev + c Vcur (in column col)
+          const double zp = Z[kp - 1];
+          const double r = hypot(zp, z);
+          const double c = z / r, sn = zp / r;
+          const int cp = CI[kp - 1];
+          for (int t2 = a; t2 < hi; ++t2) {
+            const double vp = S[(size_t)cp * k + t2], vc = S[(size_t)col * k + t2];
+            S[(size_t)cp * k + t2] = c * vp - sn * vc;
+            S[(size_t)col * k + t2] = sn * vp + c * vc;
+          }
+          --dp;
+          D[dp] = D[kp - 1];
+          CI[dp] = cp;
+          D[kp - 1] = d;
+          Z[kp - 1] = r;
+          NF[kp - 1] = r * r;
+          CI[kp - 1] = col;
+        } else {
+          D[kp] = d;
+          Z[kp] = z;
+          NF[kp] = z * z;
+          CI[kp] = col;
+          ++kp;
+        }
+      }
+      for (int u = dp, v = hi - 1; u < v; ++u, --v) {
+        const double tmp = D[u];
+        D[u] = D[v];
+        D[v] = tmp;
+        const int ti = CI[u];
+        CI[u] = CI[v];
+        CI[v] = ti;
+      }
+      for (int u = dp + 1; u < hi; ++u) {
+        const double dv = D[u];
+        const int cv = CI[u];
+        int v = u - 1;
+        while (v >= dp && D[v] > dv) {
+          D[v + 1] = D[v];
+          CI[v + 1] = CI[v];
+          --v;
+        }
+        D[v + 1] = dv;
+        CI[v + 1] = cv;
+      }
+      const int mk = kp - a;
+      MS[q] = mk | (flip ? kFlipBit : 0);
+      RH[q] = rho;
+      UB[q] = mk > 0 ? D[kp - 1] + rho * zs * (1.0 + 16.0 * DBL_EPSILON) +
+                           16.0 * DBL_EPSILON * fabs(D[kp - 1])
+                     : 0.0;
+    }
+    __syncthreads();
+    ok &= span > kDcNarrow ? dc_merge_roots<4, true>(Ar, k, s, nm, U)
+                           : dc_merge_roots<1, true>(Ar, k, s, nm, U);
+    // D': the merged columns into S2 (rows a..hi-1)
+    for (int idx = tid; idx < nm * span * span; idx += nt) {
+      const int q = idx / (span * span);
+      const int rem = idx - q * span * span;
+      const int j = rem / span, tt = rem - j * span;
+      const int a = q * span, hi = min(a + span, k);
+      const int c = a + j, t = a + tt;
+      if (c >= hi || t >= hi) continue;
+      const int mk = MS[q] & (kFlipBit - 1);
+      if (j < mk) {
+        const double *u = U + (size_t)c * k;
+        double acc = 0.0;
+        for (int i = 0; i < mk; ++i) acc = fma(u[i], S[(size_t)CI[a + i] * k + t], acc);
+        S2[(size_t)c * k + t] = acc;
+      } else {
+        S2[(size_t)c * k + t] = S[(size_t)CI[c] * k + t];
+      }
+    }
+    // E: ascending merge of the roots [a, a+mk) and the dropped poles
+    // [a+mk, hi); a negated merge is negated back and reversed
+    for (int q = tid; q < nm; q += nt) {
+      const int a = q * span, hi = min(a + span, k);
+      const int mk = MS[q] & (kFlipBit - 1);
+      const bool flip = (MS[q] & kFlipBit) != 0;
+      const double sg = flip ? -1.0 : 1.0;
+      int c1 = a, c2 = a + mk;
+      for (int t = 0; t < hi - a; ++t) {
+        double v;
+        int src;
+        if (c1 < a + mk && (c2 >= hi || X[c1] <= D[c2])) {
+          v = X[c1];
+          src = c1++;
+        } else {
+          v = D[c2];
+          src = c2++;
+        }
+        const int pos = flip ? hi - 1 - t : a + t;
+        LAM[pos] = sg * v;
+        O[pos] = src;
+      }
+    }
+    __syncthreads();
+    for (int idx = tid; idx < nm * span * span; idx += nt) {
+      const int q = idx / (span * span);
+      const int rem = idx - q * span * span;
+      const int j = rem / span, tt = rem - j * span;
+      const int a = q * span, hi = min(a + span, k);
+      const int c = a + j, t = a + tt;
+      if (c >= hi || t >= hi) continue;
+      S[(size_t)c * k + t] = S2[(size_t)O[c] * k + t];
+    }
+    __syncthreads();
+  }
+  ok = __syncthreads_and(ok) != 0;
+  for (int j = tid; j < k; j += nt) w_out[(size_t)b * k + j] = ok ? LAM[j] : nan("");
+  double *Sb = S_out + (size_t)b * k * k;
+  for (int idx = tid; idx < k * k; idx += nt) {
+    const int row = idx / k, j = idx - row * k;
+    Sb[idx] = S[(size_t)j * k + row];
+  }
+  if (!ok && tid == 0 && status) atomicExch(status, (int)MFG_ERR_NO_CONVERGENCE);
+}
+
 int launch_tridiag_quadrature(int64_t k, int64_t p, const double *H, int32_t fun, double param,
                               const double *scale, double *values, double *eigvals,
                               double *first_sq, int *status, cudaStream_t s) {
@@ -884,6 +1120,22 @@ int launch_mean_sem(const double *values, int64_t p, double *mean_sem, cudaStrea
   if (p <= 0) return MFG_ERR_BAD_ARG;
   mean_sem_kernel<<<1, kThreads, 0, s>>>(values, p, mean_sem);
   return MFG_LAUNCH_STATUS();
+}
+
+// Every eigenvector: divide and conquer for kDcMinK <= k <= kDcvMaxK (the
+// gradient's k), implicit QL otherwise.
+int launch_tridiag_eigh_full(int64_t k, int64_t p, const double *H, double *w, double *S,
+                             double *Z, int *status, cudaStream_t s) {
+  if (p <= 0 || k <= 0) return MFG_OK;
+  if (k >= kDcMinK && k <= kDcvMaxK) {
+    const size_t smem = dcv_smem_bytes((int)k);
+    MFG_CUDA_TRY(cudaFuncSetAttribute(tridiag_dcv_kernel,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int threads = (int)((4 * k + 31) / 32 * 32);
+    tridiag_dcv_kernel<<<(unsigned)p, threads, smem, s>>>((int)k, p, H, w, S, status);
+    return MFG_LAUNCH_STATUS();
+  }
+  return launch_tridiag_eigh_ql(k, p, H, w, S, Z, status, s);
 }
 
 }  // namespace mfg

@@ -8,9 +8,9 @@ It checks the algorithm the kernel implements on the CPU: eigenvalues to
 tridiagonals.
 
 ``dc_full`` runs the same merges carrying whole eigenvector columns instead of
-their first and last rows (the form that would replace the implicit-QL
-eigenvector kernel of the gradient's Daleckii-Krein term): S^T S = I and
-S diag(lambda) S^T = T to 1e-12 k on the same spectra.
+their first and last rows (tridiag_dcv_kernel, the eigenvectors of the
+gradient's Daleckii-Krein term): S^T S = I and S diag(lambda) S^T = T to
+1e-12 k on the same spectra.
 """
 
 import math
