@@ -141,3 +141,34 @@ def test_pytree_ravel_roundtrip():
     assert torch.equal(back["a"], tree["a"]) and torch.equal(back["b"][0], tree["b"][0])
     batched = unravel(torch.stack([flat, 2 * flat]))
     assert batched["b"][0].shape == (2, 2, 2)
+
+
+def test_serve_footprint_grows_with_every_dimension():
+    from matfree_gb300 import serve
+
+    base = serve.footprint_bytes(4096, 32, 64, "bf16x3")
+    assert base > 4 * 4096 * 4096  # at least the bf16 hi + lo operator (2 + 2 bytes)
+    assert serve.footprint_bytes(8192, 32, 64, "bf16x3") > base
+    assert serve.footprint_bytes(4096, 64, 64, "bf16x3") > base
+    assert serve.footprint_bytes(4096, 32, 128, "bf16x3") > base
+    assert serve.footprint_bytes(4096, 32, 64, "bf16") < base
+
+
+def test_serve_request_stream_is_seeded():
+    from matfree_gb300 import serve
+
+    a = serve.synthetic_stream(20, rate=50.0, seed=3)
+    b = serve.synthetic_stream(20, rate=50.0, seed=3)
+    assert [(len(r.x), r.k, r.p, r.fun, r.arrival) for r in a] == \
+        [(len(r.x), r.k, r.p, r.fun, r.arrival) for r in b]
+    assert all(512 <= len(r.x) <= 32768 and r.k in (16, 32, 64, 96) for r in a)
+    assert all(t1.arrival < t2.arrival for t1, t2 in zip(a, a[1:]))
+
+
+def test_serve_function_names():
+    from matfree_gb300 import _lib, serve
+
+    assert serve._fun_code("log") == (_lib.MFG_FUN_LOG, 0.0)
+    assert serve._fun_code("exp:-0.1") == (_lib.MFG_FUN_EXP, -0.1)
+    with pytest.raises(ValueError, match="unknown matrix function"):
+        serve._fun_code("sqrt")
