@@ -172,3 +172,22 @@ def test_serve_function_names():
     assert serve._fun_code("exp:-0.1") == (_lib.MFG_FUN_EXP, -0.1)
     with pytest.raises(ValueError, match="unknown matrix function"):
         serve._fun_code("sqrt")
+
+
+def test_eigh_and_adjoint_argument_errors_without_gpu():
+    lib = _lib.lib()
+    buf = ctypes.c_void_p(4096)
+    # mfg_tridiag_eigh: sizes and pointers are checked before any launch
+    assert lib.mfg_tridiag_eigh(0, 1, buf, buf, buf, buf, None) == _lib.MFG_ERR_BAD_ARG
+    assert lib.mfg_tridiag_eigh(4, 0, buf, buf, buf, buf, None) == _lib.MFG_ERR_BAD_ARG
+    assert lib.mfg_tridiag_eigh(4, 1, None, buf, buf, buf, None) == _lib.MFG_ERR_BAD_ARG
+    # mfg_hessenberg_adjoint: k = 0 is a range error (decomp.py:483-486), missing outputs bad args
+    A = _lib.MfgOperator()
+    A.kind, A.precision, A.n, A.lda, A.a = _lib.MFG_OP_DENSE, _lib.MFG_PREC_FP64, 16, 16, 4096
+    args = (buf, buf, buf, buf, buf, None, None, buf, buf, buf, 1 << 20, None)
+    assert lib.mfg_hessenberg_adjoint(ctypes.byref(A), 0, 1, 16, *args) == _lib.MFG_ERR_RANGE
+    assert lib.mfg_hessenberg_adjoint(ctypes.byref(A), 17, 1, 16, *args) == _lib.MFG_ERR_RANGE
+    bad = (None,) + args[1:]
+    assert lib.mfg_hessenberg_adjoint(ctypes.byref(A), 4, 1, 16, *bad) == _lib.MFG_ERR_BAD_ARG
+    small_ws = args[:-2] + (16, None)
+    assert lib.mfg_hessenberg_adjoint(ctypes.byref(A), 4, 1, 16, *small_ws) == _lib.MFG_ERR_WORKSPACE
