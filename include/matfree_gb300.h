@@ -161,22 +161,24 @@ MFG_API int mfg_hessenberg_adjoint(const mfg_operator *op, int64_t k, int64_t p,
                                    const double *dc, void *Lambda, void *dv, void *workspace,
                                    size_t workspace_bytes, void *stream);
 
+/* Eigenvalues (ascending, eigvals p x k) and every eigenvector (eigvecs p
+ * k x k, row-major, column j = eigenvector j) of the symmetric tridiagonal
+ * part of (H + H^T)/2 for p Hessenberg matrices, in float64: divide and
+ * conquer (one CTA per problem) for 16 <= k <= 64, implicit QL (one warp per
+ * problem) otherwise; scratch holds p k x k doubles (used by the QL form).
+ * The dense eigh that the derivative of e1^T f(T) e1 uses
+ * (matfree/funm.py:322-335 under autodiff). */
+MFG_API int mfg_tridiag_eigh(int64_t k, int64_t p, const double *H, double *eigvals,
+                             double *eigvecs, double *scratch, void *stream);
+
 /* For each of p Hessenberg matrices: T = (H + H^T)/2 restricted to its
- * tridiagonal part, eigenvalues by implicit QL in float64 with the first
- * eigenvector components tracked (Golub-Welsch), and
+ * tridiagonal part, its eigenvalues and the squares of the first eigenvector
+ * components in float64 -- divide and conquer for 16 <= k <= 2048, implicit
+ * QL with the first components tracked (Golub-Welsch) otherwise -- and
  * values[b] = scale[b] * sum_i f(lambda_i) s_1i^2.  eigvals / first_sq may be
  * NULL; scale may be NULL (1).
  * Replaces funm.dense_funm_sym_eigh + the quadform's e1^T f(T) e1
  * (matfree/funm.py:239-241, 322-335) and decomp.py:133-135. */
-/* Eigenvalues (ascending, eigvals p x k) and every eigenvector (eigvecs p
- * k x k, row-major, column j = eigenvector j) of the symmetric tridiagonal
- * part of (H + H^T)/2 for p Hessenberg matrices (implicit QL, one warp per
- * problem); scratch holds p k x k doubles.  The dense eigh that the
- * derivative of e1^T f(T) e1 uses (matfree/funm.py:322-335 under
- * autodiff). */
-MFG_API int mfg_tridiag_eigh(int64_t k, int64_t p, const double *H, double *eigvals,
-                             double *eigvecs, double *scratch, void *stream);
-
 MFG_API int mfg_tridiag_quadrature(int64_t k, int64_t p, const double *H, int32_t fun,
                            double param, const double *scale, double *values,
                            double *eigvals, double *first_sq, void *stream);
