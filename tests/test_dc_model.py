@@ -287,3 +287,135 @@ def test_dc_full_vectors_match_eigh(kind, k):
     np.testing.assert_allclose(lam, np.linalg.eigvalsh(T), rtol=0, atol=1e-12 * scale)
     np.testing.assert_allclose(S.T @ S, np.eye(k), atol=1e-12 * k)
     np.testing.assert_allclose((S * lam) @ S.T, T, atol=1e-12 * k * scale)
+
+
+# ---------------------------------------------------------------------------
+# The eigenvector kernel's own index arithmetic (column-index array CI, in-place
+# close-pole rotations, the S2 staging and the column map O), run phase by
+# phase with the threads of a phase one after another: a phase's threads touch
+# disjoint entries, so the order does not matter.  Roots come from the scalar
+# secular solver above; everything else follows the CUDA source line by line.
+
+def dcv_kernel_phases(H):
+    """tridiag_dcv_kernel phase by phase, threads run one after another."""
+    k = H.shape[0]
+    EO = np.array([0.5 * (H[i, i + 1] + H[i + 1, i]) if i + 1 < k else 0.0 for i in range(k)])
+    LAM = np.array([H[i, i] - (EO[i - 1] if i > 0 else 0.0) - EO[i] for i in range(k)])
+    S = np.zeros(k * k); S2 = np.zeros(k * k); U = np.zeros(k * k)
+    for i in range(k): S[i * k + i] = 1.0
+    D = np.zeros(k); Z = np.zeros(k); X = np.zeros(k); NF = np.zeros(k)
+    CI = np.zeros(k, dtype=int); O = np.zeros(k, dtype=int)
+    kh = (k + 1) // 2
+    MS = np.zeros(kh, dtype=int); RH = np.zeros(kh); UB = np.zeros(kh)
+    FLIP = 1 << 30
+    ok = True
+    s = 0
+    while (1 << s) < k:
+        w = 1 << s; span = 2 * w; nm = (k - w - 1) // span + 1
+        # A
+        for q in range(nm):
+            a = q * span; mid = a + w; hi = min(a + span, k)
+            rho = EO[mid - 1]; flip = rho < 0.0; sg = -1.0 if flip else 1.0; rho = abs(rho)
+            maxabs = max(abs(LAM[a]), abs(LAM[mid - 1]), abs(LAM[mid]), abs(LAM[hi - 1]))
+            tol = 8.0 * EPS * max(maxabs, 2.0 * rho)
+            n1, n2 = mid - a, hi - mid
+            c1 = c2 = 0; kp = a; dp = hi; zs = 0.0
+            for t in range(a, hi):
+                if c1 == n1: take1 = False
+                elif c2 == n2: take1 = True
+                else: take1 = sg * LAM[mid - 1 - c1 if flip else a + c1] <= sg * LAM[hi - 1 - c2 if flip else mid + c2]
+                if take1:
+                    col = mid - 1 - c1 if flip else a + c1; z = S[col * k + (mid - 1)]; c1 += 1
+                else:
+                    col = hi - 1 - c2 if flip else mid + c2; z = S[col * k + mid]; c2 += 1
+                d = sg * LAM[col]
+                if rho * abs(z) <= tol:
+                    dp -= 1; D[dp] = d; CI[dp] = col; continue
+                zs = zs + z * z
+                if kp > a and d - D[kp - 1] <= tol:
+                    zp = Z[kp - 1]; r = math.hypot(zp, z); c = z / r; sn = zp / r; cp = CI[kp - 1]
+                    for t2 in range(a, hi):
+                        vp, vc = S[cp * k + t2], S[col * k + t2]
+                        S[cp * k + t2] = c * vp - sn * vc
+                        S[col * k + t2] = sn * vp + c * vc
+                    dp -= 1; D[dp] = D[kp - 1]; CI[dp] = cp
+                    D[kp - 1] = d; Z[kp - 1] = r; NF[kp - 1] = r * r; CI[kp - 1] = col
+                else:
+                    D[kp] = d; Z[kp] = z; NF[kp] = z * z; CI[kp] = col; kp += 1
+            u, v = dp, hi - 1
+            while u < v:
+                D[u], D[v] = D[v], D[u]; CI[u], CI[v] = CI[v], CI[u]; u += 1; v -= 1
+            for u in range(dp + 1, hi):
+                dv, cv = D[u], CI[u]; v = u - 1
+                while v >= dp and D[v] > dv:
+                    D[v + 1] = D[v]; CI[v + 1] = CI[v]; v -= 1
+                D[v + 1] = dv; CI[v + 1] = cv
+            mk = kp - a
+            MS[q] = mk | (FLIP if flip else 0); RH[q] = rho
+            UB[q] = D[kp - 1] + rho * zs * (1.0 + 16.0 * EPS) + 16.0 * EPS * abs(D[kp - 1]) if mk > 0 else 0.0
+        # B, C, D (roots via the model's secular solver, zhat, U)
+        for q in range(nm):
+            a = q * span; mk = MS[q] & (FLIP - 1)
+            P = D[a:a + mk].copy(); ZZ = NF[a:a + mk].copy()
+            xs = []
+            for j in range(mk):
+                x, o, conv = _secular(list(P), list(ZZ), mk, j, RH[q], UB[q]); ok &= conv
+                xs.append((x, o)); X[a + j] = x; O[a + j] = o
+            for i in range(mk):
+                di = P[i]
+                prod = ((P[O[a + mk - 1]] - di) + X[a + mk - 1]) / RH[q]
+                for j in range(mk - 1):
+                    prod *= ((P[O[a + j]] - di) + X[a + j]) / (P[j if j < i else j + 1] - di)
+                Z[a + i] = math.copysign(math.sqrt(max(prod, 0.0)), Z[a + i])
+            for j in range(mk):
+                r = a + j; ox = P[O[r]]; x = X[r]
+                us = [Z[a + i] / ((P[i] - ox) - x) for i in range(mk)]
+                rn = 1.0 / math.sqrt(sum(u * u for u in us))
+                for i in range(mk): U[r * k + i] = us[i] * rn
+                X[r] = ox + x
+        # D'
+        for idx in range(nm * span * span):
+            q = idx // (span * span); rem = idx - q * span * span; j = rem // span; tt = rem - j * span
+            a = q * span; hi = min(a + span, k); c = a + j; t = a + tt
+            if c >= hi or t >= hi: continue
+            mk = MS[q] & (FLIP - 1)
+            if j < mk:
+                acc = 0.0
+                for i in range(mk): acc += U[c * k + i] * S[CI[a + i] * k + t]
+                S2[c * k + t] = acc
+            else:
+                S2[c * k + t] = S[CI[c] * k + t]
+        # E
+        for q in range(nm):
+            a = q * span; hi = min(a + span, k); mk = MS[q] & (FLIP - 1); flip = (MS[q] & FLIP) != 0
+            sg = -1.0 if flip else 1.0; c1 = a; c2 = a + mk
+            for t in range(hi - a):
+                if c1 < a + mk and (c2 >= hi or X[c1] <= D[c2]):
+                    v = X[c1]; src = c1; c1 += 1
+                else:
+                    v = D[c2]; src = c2; c2 += 1
+                pos = hi - 1 - t if flip else a + t
+                LAM[pos] = sg * v; O[pos] = src
+        for idx in range(nm * span * span):
+            q = idx // (span * span); rem = idx - q * span * span; j = rem // span; tt = rem - j * span
+            a = q * span; hi = min(a + span, k); c = a + j; t = a + tt
+            if c >= hi or t >= hi: continue
+            S[c * k + t] = S2[O[c] * k + t]
+        s += 1
+    Sout = S.reshape(k, k).T.copy()  # Sb[row*k + j] = S[j*k + row]
+    return LAM, Sout, ok
+
+
+@pytest.mark.parametrize("kind", ["normal", "wilkinson", "glued", "split", "tiny", "negative", "zero"])
+@pytest.mark.parametrize("k", [16, 20, 33, 48, 64])
+def test_dcv_kernel_phases_match_eigh(kind, k):
+    rng = np.random.default_rng(1000 * k + sum(map(ord, kind)))
+    d, e = _case(kind, k, rng)
+    H = np.diag(d) + np.diag(e, 1) + np.diag(e, -1)
+    lam, S, ok = dcv_kernel_phases(H)
+    assert ok
+    w0 = np.linalg.eigvalsh(H)
+    scale = max(np.abs(w0).max(), 1e-300)
+    np.testing.assert_allclose(lam, w0, rtol=0, atol=1e-12 * scale)
+    np.testing.assert_allclose(S.T @ S, np.eye(k), atol=1e-12 * k)
+    np.testing.assert_allclose((S * lam) @ S.T, H, atol=1e-12 * k * scale)
