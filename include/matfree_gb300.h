@@ -311,25 +311,40 @@ MFG_API int mfg_split_bf16(const float *a, int64_t rows, int64_t cols, int64_t l
                    void *hi, void *lo, int64_t ld_out, void *stream);
 
 /* Operator application that allocates nothing: the same W = (A + shift I) V
- * as mfg_operator_apply, for callers that cannot allocate device memory
- * (code running inside another framework's memory pool, an allocator-free
- * embedded host, or a CUDA stream capture where allocation is not allowed)
- * and therefore cannot provide a workspace.  It has no counterpart in the
- * reference (matfree is JAX and never manages device memory itself).
+ * as mfg_operator_apply, for callers that cannot allocate device memory and
+ * therefore cannot provide a workspace -- code running inside another
+ * framework's fixed memory pool (where a second allocator would fight the
+ * pool's own accounting), or an embedded host without a device allocator.
+ * It has no counterpart in the reference (matfree is JAX and never manages
+ * device memory itself).
  *
- * The only scratch it needs, the bf16 hi/lo copies of the probe panel for
- * the tensor-core precisions, lives in one fixed array inside this library:
+ * The only scratch it needs lives in one fixed array inside this library:
  * MFG_NOALLOC_SCRATCH_BYTES (32 MiB) of device memory that every GPU which
- * loads the library holds until the process exits.  Panels needing more
- * (p * ld * 4 bytes > 32 MiB for bf16x3, p * ld * 2 bytes for bf16) are
- * rejected with MFG_ERR_SCRATCH_LIMIT before any work is queued.  The first
- * call on a device looks up that device's copy of the array (no allocation);
- * make that first call before any stream capture.  All calls share the one
- * array: calls that overlap on the GPU (other streams, other threads) race
- * on it and must be serialised by the caller. */
+ * loads the library holds until the process exits.  Its layout is a 256-byte
+ * status word, then the bf16 hi copy of the panel, then (bf16x3) the bf16 lo
+ * copy, each copy padded to a multiple of 256 bytes.  A call is rejected with
+ * MFG_ERR_SCRATCH_LIMIT, before any work is queued, when
+ *     256 + copies * round_up(p * ld * 2, 256) > MFG_NOALLOC_SCRATCH_BYTES
+ * with copies = 2 for MFG_PREC_BF16X3, 1 for MFG_PREC_BF16 and 0 otherwise
+ * (fp32, fp64 and CSR need no panel copy and are never rejected for size).
+ * The first call on a device looks up that device's copy of the array (no
+ * allocation); make that first call before any stream capture.  All calls
+ * share the one array and the status word is cleared at the start of each
+ * call: calls that overlap on the GPU (other streams, other threads) race on
+ * it and must be serialised by the caller.
+ *
+ * The return code reports launch-time errors only.  A bounded device-side
+ * wait that gives up (MFG_ERR_TIMEOUT; the product is then left incomplete)
+ * is recorded in the status word and is otherwise silent: read it with
+ * mfg_operator_apply_noalloc_status. */
 #define MFG_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
 MFG_API int mfg_operator_apply_noalloc(const mfg_operator *op, const void *V, void *W,
                                        int64_t p, int64_t ld, void *stream);
+
+/* Waits for `stream` and returns the device-side status of the most recent
+ * mfg_operator_apply_noalloc on the current device (MFG_OK or
+ * MFG_ERR_TIMEOUT), or a host error code.  Allocates nothing. */
+MFG_API int mfg_operator_apply_noalloc_status(void *stream);
 
 #ifdef __cplusplus
 }

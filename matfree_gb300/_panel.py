@@ -19,9 +19,32 @@ def padded_ld(n: int) -> int:
     return (int(n) + 7) // 8 * 8
 
 
-def require_cuda(t: torch.Tensor, what: str) -> None:
-    if not isinstance(t, torch.Tensor) or not t.is_cuda:
+def as_tensor(x, what: str):
+    """A torch view of a torch tensor or of any array that exports its memory
+    through DLPack (``__dlpack__``) or ``__cuda_array_interface__`` (CuPy, JAX,
+    Numba, ...): no copy is made, the producer keeps ownership."""
+    if isinstance(x, torch.Tensor):
+        return x
+    if hasattr(x, "__dlpack__"):
+        try:
+            return torch.from_dlpack(x)
+        except Exception as err:  # noqa: BLE001  (producer-specific failures)
+            raise TypeError(f"{what}: DLPack import failed ({err})") from err
+    if hasattr(x, "__cuda_array_interface__"):
+        return torch.as_tensor(x, device="cuda")
+    if type(x).__name__ == "PyCapsule":
+        return torch.utils.dlpack.from_dlpack(x)
+    raise TypeError(f"{what} must be a CUDA tensor or a DLPack-capable CUDA array "
+                    f"(matfree_gb300 runs on the GPU only); got {type(x).__name__}")
+
+
+def require_cuda(t, what: str) -> torch.Tensor:
+    """Return ``t`` as a torch CUDA tensor (DLPack producers are imported
+    without a copy); raise TypeError for host arrays and unknown objects."""
+    t = as_tensor(t, what)
+    if not t.is_cuda:
         raise TypeError(f"{what} must be a CUDA tensor (matfree_gb300 runs on the GPU only)")
+    return t
 
 
 def stream_ptr() -> ctypes.c_void_p:
@@ -46,7 +69,7 @@ def as_panel(x: torch.Tensor, n: int, dtype) -> tuple[torch.Tensor, int]:
     Reuses x's storage when its layout already qualifies and the padding
     columns are not read as data (the kernels mask every column >= n).
     """
-    require_cuda(x, "probe/vector panel")
+    x = require_cuda(x, "probe/vector panel")
     if x.dtype == dtype and is_panel(x, n):
         ld = x.stride(0) if x.shape[0] > 1 else padded_ld(n)
         return x, ld

@@ -197,8 +197,8 @@ def rbf_logdet(x: torch.Tensor, theta: torch.Tensor, probes: torch.Tensor, num_m
     theta = (log s2, log ell, log tau) as a CUDA or CPU tensor of 3 values;
     probes (p, n) CUDA tensor; returns a 0-d float64 tensor.
     """
-    require_cuda(x, "x")
-    require_cuda(probes, "probes")
+    x = require_cuda(x, "x")
+    probes = require_cuda(probes, "probes")
     if num_matvecs <= 0 or num_matvecs > x.shape[0]:
         from .decomp import _error_num_matvecs
 

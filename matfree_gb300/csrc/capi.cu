@@ -1079,6 +1079,16 @@ int mfg_operator_apply_noalloc(const mfg_operator *op, const void *V, void *W, i
   return apply_op<float>(op, (const float *)V, ld, (float *)W, ld, p, hi, lo, ld, nullptr, status, s);
 }
 
+int mfg_operator_apply_noalloc_status(void *stream) {
+  void *base = nullptr;
+  MFG_TRY(noalloc_scratch(&base));
+  cudaStream_t s = as_stream(stream);
+  int word = 0;
+  MFG_CUDA_TRY(cudaMemcpyAsync(&word, base, sizeof(int), cudaMemcpyDeviceToHost, s));
+  MFG_CUDA_TRY(cudaStreamSynchronize(s));
+  return word;
+}
+
 int mfg_hessenberg(const mfg_operator *op, int64_t k, int64_t p, const void *V, int64_t ld,
                    int32_t reortho, void *Q, double *H, void *residual, double *init_len_inv,
                    void *workspace, size_t workspace_bytes, void *stream) {

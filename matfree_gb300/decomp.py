@@ -63,7 +63,7 @@ def run_hessenberg(op, k: int, V: torch.Tensor, *, reortho: str = "full", worksp
     "lanczos" (the three-term recurrence).
     Returns (Q (p, k, n), H (p, k, k) float64, residual (p, n), 1/||v|| (p,)).
     """
-    require_cuda(V, "vectors")
+    V = require_cuda(V, "vectors")
     n = op.n
     p = V.shape[0]
     if k < 0 or k > n:
@@ -123,7 +123,7 @@ class _Decomposition:
         n = flat.numel()
         if self.num_matvecs < 0 or self.num_matvecs > n:
             raise ValueError(_error_num_matvecs(self.num_matvecs, maxval=n, minval=0))
-        require_cuda(flat, "vec")
+        flat = require_cuda(flat, "vec")
         op = _flat_operator(matvec, unravel, n, flat.dtype, params)
         return flat, unravel, op
 
@@ -270,7 +270,7 @@ class _Bidiag:
         Returns (U (p, k, n_rows), V (p, k, n_cols), alphas (p, k), betas (p, k),
         residual (p, n_cols), 1/||v0|| (p,)); betas[:, 0] = 0 as in matfree.
         """
-        require_cuda(V0, "V0")
+        V0 = require_cuda(V0, "V0")
         p, ncols = V0.shape
         A, At, nrows, _ = self._operators(Av, V0[0], params)
         k = self.num_matvecs
@@ -310,7 +310,7 @@ class _Bidiag:
         from .operators import Operator
 
         flat, unravel = ravel_pytree(v0)
-        require_cuda(flat, "v0")
+        flat = require_cuda(flat, "v0")
         if isinstance(Av, Operator):
             U, V, alphas, betas, R, c = self.batched(Av, flat[None, :], *params)
             out_like, u_unravel = flat, unravel

@@ -47,7 +47,7 @@ class DenseFunmSymEigh:
         self.param = float(param)
 
     def __call__(self, dense_matrix: torch.Tensor) -> torch.Tensor:
-        require_cuda(dense_matrix, "dense_matrix")
+        dense_matrix = require_cuda(dense_matrix, "dense_matrix")
         w, V = torch.linalg.eigh(dense_matrix)
         return V @ torch.diag_embed(self.apply_scalar(w)) @ V.transpose(-1, -2)
 
@@ -94,13 +94,13 @@ class MonteCarloFunmSym:
     # single vector: the matfree call signature
     def __call__(self, matvec, v0, *parameters):
         flat, unravel = ravel_pytree(v0)
-        require_cuda(flat, "v0")
+        flat = require_cuda(flat, "v0")
         op = _flat_operator(matvec, unravel, flat.numel(), flat.dtype, parameters)
         return self.batched(op, flat[None, :])[0]
 
     def batched(self, matvec, samples: torch.Tensor, *parameters) -> torch.Tensor:
         """Integrand values (p,) float64 for the rows of samples (p, n)."""
-        require_cuda(samples, "samples")
+        samples = require_cuda(samples, "samples")
         p, n = samples.shape
         k = self.tridiag_sym.num_matvecs
         if isinstance(matvec, Operator):
@@ -224,7 +224,7 @@ def funm_lanczos_sym(dense_funm, tridiag_sym, /):
 
     def estimate(matvec, vec, *parameters):
         flat, unravel = ravel_pytree(vec)
-        require_cuda(flat, "vec")
+        flat = require_cuda(flat, "vec")
         length = torch.linalg.vector_norm(flat)
         Q, T, *_ = tridiag_sym(_flat_operator(matvec, unravel, flat.numel(), flat.dtype, parameters)
                                if not isinstance(matvec, Operator) else matvec, flat / length)
@@ -251,7 +251,7 @@ class DenseFunmProductSvd(DenseFunmSymEigh):
     """
 
     def __call__(self, matrix: torch.Tensor) -> torch.Tensor:
-        require_cuda(matrix, "matrix")
+        matrix = require_cuda(matrix, "matrix")
         _, S, Vt = torch.linalg.svd(matrix)
         eigvecs = Vt.transpose(-1, -2)
         return eigvecs @ torch.diag_embed(self.apply_scalar(S * S)) @ eigvecs.transpose(-1, -2)
@@ -277,7 +277,7 @@ class MonteCarloFunmProduct:
 
     def __call__(self, matvec, v0, *parameters):
         flat, unravel = ravel_pytree(v0)
-        require_cuda(flat, "v0")
+        flat = require_cuda(flat, "v0")
         if isinstance(matvec, Operator):
             return self.batched(matvec, flat[None, :], *parameters)[0]
 
@@ -288,7 +288,7 @@ class MonteCarloFunmProduct:
 
     def batched(self, matvec, samples: torch.Tensor, *parameters) -> torch.Tensor:
         """Integrand values (p,) float64 for the rows of samples (p, n_cols)."""
-        require_cuda(samples, "samples")
+        samples = require_cuda(samples, "samples")
         k = self.bidiag.num_matvecs
         if self.dense_funm.kind is not None:
             return _slq_product_values(self.bidiag, matvec, samples, k, self.dense_funm.kind,

@@ -81,8 +81,8 @@ def rbf_logpdf(x: torch.Tensor, theta: torch.Tensor, y: torch.Tensor, probes: to
     observations, probes (p, n) CUDA Rademacher probes of the log-determinant.
     Returns a 0-d float64 tensor.
     """
-    require_cuda(x, "x")
-    require_cuda(y, "y")
+    x = require_cuda(x, "x")
+    y = require_cuda(y, "y")
     n = x.shape[0]
     quad = _RBFQuad.apply(theta, x.to(torch.float32).contiguous(), y.reshape(-1), precision, cg_tol)
     logdet = rbf_logdet(x, theta, probes, num_matvecs, precision=precision)

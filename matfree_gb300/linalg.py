@@ -27,7 +27,7 @@ _WS = Workspace()
 def cg_batched(op, B: torch.Tensor, *, tol: float = 1e-5, atol: float = 0.0, maxiter=None,
                workspace=None):
     """Solve op X_b = B_b for every row b of B (p, n); returns (X (p, n), iterations (p,))."""
-    require_cuda(B, "B")
+    B = require_cuda(B, "B")
     if B.dim() != 2:
         raise ValueError("B must be a (p, n) panel")
     p, n = B.shape
@@ -65,6 +65,6 @@ def cg(A, b: torch.Tensor, x0=None, *, tol: float = 1e-5, atol: float = 0.0, max
         raise NotImplementedError("preconditioned CG is not supported")
     if x0 is not None and bool(torch.any(x0 != 0)):
         raise NotImplementedError("CG starts from x0 = 0")
-    require_cuda(b, "b")
+    b = require_cuda(b, "b")
     X, _ = cg_batched(A, b.reshape(1, -1), tol=tol, atol=atol, maxiter=maxiter)
     return X[0].reshape(b.shape), None

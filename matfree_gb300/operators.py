@@ -46,7 +46,7 @@ class Operator:
         """Apply to the rows of V (p, n); returns (p, n)."""
         from ._panel import as_panel
 
-        require_cuda(V, "V")
+        V = require_cuda(V, "V")
         p = V.shape[0]
         panel, ld = as_panel(V, self.n, self.basis_dtype)
         out = torch.zeros((p, ld), dtype=self.basis_dtype, device=V.device)
@@ -79,7 +79,7 @@ class DenseOperator(Operator):
     """
 
     def __init__(self, A: torch.Tensor, *, precision: str = "fp32", shift: float = 0.0):
-        require_cuda(A, "A")
+        A = require_cuda(A, "A")
         if A.dim() != 2 or A.shape[0] != A.shape[1]:
             raise ValueError("A must be square")
         if precision not in _lib.PRECISIONS:
@@ -160,7 +160,7 @@ class RBFKernelOperator(DenseOperator):
 
     def __init__(self, x: torch.Tensor, *, s2: float = 1.0, ell: float = 0.2, tau: float = 1e-2,
                  precision: str = "bf16x3"):
-        require_cuda(x, "x")
+        x = require_cuda(x, "x")
         if precision not in _lib.PRECISIONS:
             raise ValueError(f"precision must be one of {sorted(_lib.PRECISIONS)}")
         x = x.to(torch.float32).contiguous()
@@ -194,8 +194,9 @@ class CSROperator(Operator):
     """A + shift I for a CSR matrix (int32 row_ptr / col_idx, float32 values)."""
 
     def __init__(self, row_ptr, col_idx, values, n: int, *, shift: float = 0.0):
-        for t, name in ((row_ptr, "row_ptr"), (col_idx, "col_idx"), (values, "values")):
-            require_cuda(t, name)
+        row_ptr = require_cuda(row_ptr, "row_ptr")
+        col_idx = require_cuda(col_idx, "col_idx")
+        values = require_cuda(values, "values")
         self.row_ptr = row_ptr.to(torch.int32).contiguous()
         self.col_idx = col_idx.to(torch.int32).contiguous()
         self.values = values.to(torch.float32).contiguous()

@@ -27,7 +27,7 @@ from .tree import ravel_pytree, tree_map
 class _Sampler:
     def __init__(self, kind, args_like, num):
         flat, unravel = ravel_pytree(args_like[0] if len(args_like) == 1 else args_like)
-        require_cuda(flat, "args_like")
+        flat = require_cuda(flat, "args_like")
         if flat.dtype.is_complex:
             raise NotImplementedError("complex probes (Steinhaus) are not provided by matfree_gb300")
         self.kind = kind

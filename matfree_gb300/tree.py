@@ -38,8 +38,13 @@ def tree_leaves(tree):
 
 
 def ravel_pytree(tree):
-    """Return (flat 1-D tensor, unravel) for a container of tensors."""
-    leaves = tree_leaves(tree)
+    """Return (flat 1-D tensor, unravel) for a container of tensors.
+
+    Leaves may be torch tensors or any DLPack-capable arrays (imported as
+    torch views without a copy)."""
+    from ._panel import as_tensor
+
+    leaves = [as_tensor(leaf, "pytree leaf") for leaf in tree_leaves(tree)]
     if len(leaves) == 1 and not isinstance(tree, (dict, list, tuple)):
         leaf = leaves[0]
         shape = leaf.shape

@@ -16,7 +16,7 @@ from __future__ import annotations
 
 import numpy as np
 
-from oracle import slq
+from oracle import problems, slq
 
 
 def _lower(m):
@@ -81,7 +81,7 @@ def hessenberg_adjoint_batched(vjp_matmat, nparams, *, Q, H, r, dH, c):
     lower_mask = _lower(np.ones((k, k)))
     reortho_mask = np.tril(np.ones((k, k)), 1)
     gamma = dH[:, :, k - 1]  # dH @ e_K with dr = 0
-    lam = np.einsum("pkn,pk->pn", Q, gamma)
+    lam = slq.combine(Q, gamma)
     Lam = np.zeros((p, k, n))
     Gamma = np.zeros((p, k, k))
     dp = np.zeros(nparams)
@@ -93,23 +93,20 @@ def hessenberg_adjoint_batched(vjp_matmat, nparams, *, Q, H, r, dH, c):
     beta_plus[:, idx_all, idx_all] = 0.0
     beta_plus[:, idx_all[1:], idx_all[:-1]] = 0.0
     for idx in reversed(range(k)):
-        mask = reortho_mask[idx]
-        Qm = Q * mask[None, :, None]
-        rhs = mask[None, :] * dH[:, :, idx]
-        proj = np.einsum("pkn,pn->pk", Qm, lam)
-        lam = lam - np.einsum("pkn,pk->pn", Qm, proj) + np.einsum("pkn,pk->pn", Qm, rhs)
+        # the mask row tril(1, 1)[idx] keeps columns 0..idx+1 (decomp.py:558-566)
+        m = int(reortho_mask[idx].sum())
+        Qm = Q[:, :m, :]
+        rhs = dH[:, :m, idx]
+        proj = slq.project(Qm, lam)
+        lam = lam - slq.combine(Qm, proj) + slq.combine(Qm, rhs)
         At_lam, dp_inc = vjp_matmat(Q[:, idx, :], lam)
         dp = dp + dp_inc
-        Gamma[:, idx, :] = lower_mask[idx][None, :] * (
-            Pi_gamma[:, idx, :] - np.einsum("pn,pkn->pk", At_lam, Q)
-        )
+        Gamma[:, idx, :] = lower_mask[idx][None, :] * (Pi_gamma[:, idx, :] - slq.project(Q, At_lam))
         Lam[:, idx, :] = lam
         G = Gamma[:, idx, :] + Gamma[:, :, idx]
         # Pi_xi[idx] = dQ^T[idx] + gamma[idx] r = gamma[idx] r
-        xi = gamma[:, idx, None] * r + np.einsum("pk,pkn->pn", G, Q)
-        lam = xi - (alphas[:, idx, None] * lam - At_lam) - np.einsum(
-            "pk,pkn->pn", beta_plus[:, idx, :], Lam
-        )
+        xi = gamma[:, idx, None] * r + slq.combine(Q, G)
+        lam = xi - (alphas[:, idx, None] * lam - At_lam) - slq.combine(Lam, beta_plus[:, idx, :])
         lam = lam / beta_minus[:, idx, None]
     return lam * c[:, None], dp
 
@@ -180,12 +177,19 @@ def slq_grad_batched(matmat, vjp_matmat, nparams, num_matvecs, V, f=np.log, fpri
 def rbf_matrices(x, theta):
     """Return (K, E, D) in float64 for points x (n, d) and theta=(log s2, log l, log tau)."""
     x = np.asarray(x, dtype=np.float64)
-    D = np.zeros((len(x), len(x)))
-    for d in range(x.shape[1]):
-        D += (x[:, d, None] - x[None, :, d]) ** 2
+    n = len(x)
     s2, ell, tau = np.exp(theta)
-    E = np.exp(-D / (2.0 * ell * ell))
-    K = s2 * E + tau * np.eye(len(x))
+    D = np.empty((n, n))
+    E = np.empty((n, n))
+    K = np.empty((n, n))
+
+    def fill(lo, hi):
+        D[lo:hi] = problems.sqdist_rows(x, lo, hi)
+        E[lo:hi] = np.exp(-D[lo:hi] / (2.0 * ell * ell))
+        K[lo:hi] = s2 * E[lo:hi]
+
+    problems.row_blocks(n, fill)
+    K[np.diag_indices(n)] += tau
     return K, E, D
 
 

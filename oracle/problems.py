@@ -14,6 +14,9 @@
 
 from __future__ import annotations
 
+import concurrent.futures as cf
+import os
+
 import numpy as np
 import scipy.sparse as sp
 
@@ -39,12 +42,34 @@ def rbf_points(n, seed=0, dim=3):
     return np.random.default_rng(seed).uniform(0.0, 1.0, size=(n, dim))
 
 
+def row_blocks(n, fill, rows=256, threads=None):
+    """Call fill(lo, hi) on row blocks of an n-row matrix from a thread pool
+    (NumPy releases the GIL inside its array loops, so the blocks run in
+    parallel on the host cores)."""
+    blocks = [(lo, min(n, lo + rows)) for lo in range(0, n, rows)]
+    with cf.ThreadPoolExecutor(threads or os.cpu_count() or 1) as ex:
+        list(ex.map(lambda b: fill(*b), blocks))
+
+
+def sqdist_rows(x, lo, hi):
+    """|x_i - x_j|^2 for rows lo..hi-1 against all points (float64)."""
+    D = np.zeros((hi - lo, len(x)))
+    for d in range(x.shape[1]):
+        D += (x[lo:hi, d, None] - x[None, :, d]) ** 2
+    return D
+
+
 def rbf_kernel(x, s2=1.0, ell=0.2, tau=1e-2):
     x = np.asarray(x, dtype=np.float64)
-    D = np.zeros((len(x), len(x)))
-    for d in range(x.shape[1]):
-        D += (x[:, d, None] - x[None, :, d]) ** 2
-    return s2 * np.exp(-D / (2.0 * ell * ell)) + tau * np.eye(len(x))
+    n = len(x)
+    K = np.empty((n, n))
+
+    def fill(lo, hi):
+        K[lo:hi] = s2 * np.exp(-sqdist_rows(x, lo, hi) / (2.0 * ell * ell))
+
+    row_blocks(n, fill)
+    K[np.diag_indices(n)] += tau
+    return K
 
 
 def laplacian_2d(m, shift=0.1):

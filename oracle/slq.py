@@ -168,6 +168,16 @@ def estimator_monte_carlo_mean_and_sem(integrand, matvec, samples):
 # ---------------------------------------------------------------------------
 
 
+def project(Qa, w):
+    """Q_b^T w_b for every probe b: (p, j, n), (p, n) -> (p, j) (batched BLAS GEMV)."""
+    return np.matmul(Qa, w[:, :, None])[:, :, 0]
+
+
+def combine(Qa, h):
+    """Q_b h_b for every probe b: (p, j, n), (p, j) -> (p, n) (batched BLAS GEMV)."""
+    return np.matmul(h[:, None, :], Qa)[:, 0, :]
+
+
 def hessenberg_forward_batched(matmat, num_matvecs, V, *, reortho="full"):
     """matfree/decomp.py:426-477 applied to every row of V (p, n) at once.
 
@@ -192,11 +202,11 @@ def hessenberg_forward_batched(matmat, num_matvecs, V, *, reortho="full"):
         Q[:, idx, :] = v
         w = matmat(v)
         Qa = Q[:, : idx + 1, :]
-        h = np.einsum("pin,pn->pi", Qa, w)
-        w = w - np.einsum("pin,pi->pn", Qa, h)
+        h = project(Qa, w)
+        w = w - combine(Qa, h)
         if reortho != "none":
-            h2 = np.einsum("pin,pn->pi", Qa, w)
-            w = w - np.einsum("pin,pi->pn", Qa, h2)
+            h2 = project(Qa, w)
+            w = w - combine(Qa, h2)
         length = np.sqrt(np.einsum("pn,pn->p", w, w))
         H[:, : idx + 1, idx] = h
         if idx + 1 < k:

@@ -1,0 +1,188 @@
+"""Parity at the benchmark configurations' own sizes (needs a GPU).
+
+Each case runs the CUDA path at the full n, k and p of one benchmark
+configuration and compares it with the float64 oracle (oracle/) on identical
+probe vectors; where the oracle would need more than a few tens of seconds
+or more host memory than a test should take, a stated seeded subset of the
+probes or of the requests is compared instead.  Tolerances, as the
+benchmark states them: 1e-4 relative for the split-fp32 (bf16x3) and fp32
+modes, 1e-9 for the float64 path, 1e-8 for float64 gradients.
+
+* dense1k   A = B B^T / n + I (B ~ N(0, 1), seed 0), n = 1000, k = 30,
+            p = 100, float64; also against the Cholesky log-determinant
+            within the Monte-Carlo error;
+* rbf16k    RBF kernel (x ~ U[0, 1]^3 seed 0, ell = 0.2, tau = 1e-2),
+            n = 16384, k = 64, all p = 256 probes, bf16x3 and fp32;
+* laplace1m 5-point Dirichlet Laplacian + 0.1 I on 1024 x 1024 (CSR),
+            k = 100, p = 64 on the GPU, the first 4 probes' values checked
+            (the float64 bases of all 64 would take 54 GB of host memory);
+* grad8k    d logdet / d theta for the RBF kernel at n = 8192, k = 48,
+            p = 128, theta = (0, log 0.2, log 1e-2): against the oracle's
+            adjoint and against central differences (h = 1e-4) of the
+            oracle's float64 estimate;
+* serve     whole requests (n up to 32543) of the seeded serving stream,
+            served together, each against the oracle.
+"""
+
+import math
+
+import numpy as np
+import pytest
+import torch
+
+import matfree_gb300 as mf
+from matfree_gb300 import autodiff, serve
+from oracle import adjoint as oadj
+from oracle import philox, problems, slq
+
+pytestmark = pytest.mark.gpu
+
+DEV = "cuda"
+
+
+def _t(x, dtype=torch.float64):
+    return torch.as_tensor(np.asarray(x), dtype=dtype, device=DEV)
+
+
+def _rel(got, want):
+    return abs(float(got) - float(want)) / abs(float(want))
+
+
+# ------------------------------------------------------------------ dense1k
+
+
+def test_dense1k_fp64_matches_oracle_and_cholesky():
+    n, k, p = 1000, 30, 100
+    A = problems.dense_spd(n, seed=0)
+    op = mf.DenseOperator(_t(A), precision="fp64")
+    sampler = mf.stochtrace.sampler_signs(torch.ones(n, dtype=torch.float64, device=DEV), num=p)
+    integrand = mf.funm.monte_carlo_funm_sym_logdet(mf.decomp.tridiag_sym(k))
+    key = mf.prng.prng_key(1)
+    mean, sem = mf.stochtrace.estimator_monte_carlo_mean_and_sem(integrand, sampler)(op, key)
+    V = philox.rademacher(np.asarray(key, np.uint32), p, n)
+    want = slq.slq_batched(lambda X: X @ A.T, k, V)
+    assert _rel(mean, want.mean()) <= 1e-9
+    np.testing.assert_allclose(float(sem), want.std() / math.sqrt(p), rtol=1e-7)
+    # the estimate is within its Monte-Carlo error of the exact log-determinant
+    logdet = 2.0 * np.sum(np.log(np.diag(np.linalg.cholesky(A))))
+    assert abs(float(mean) - logdet) <= 4.0 * float(sem), (float(mean), logdet, float(sem))
+
+
+# ------------------------------------------------------------------- rbf16k
+
+
+@pytest.fixture(scope="module")
+def rbf16k():
+    n, k, p = 16384, 64, 256
+    x = np.random.default_rng(0).uniform(0.0, 1.0, size=(n, 3)).astype(np.float32)
+    key = mf.prng.prng_key(1)
+    V = philox.rademacher(np.asarray(key, np.uint32), p, n)
+    K = problems.rbf_kernel(x.astype(np.float64), 1.0, 0.2, 1e-2)
+    want = slq.slq_batched(lambda X: X @ K, k, V)
+    return x, key, k, p, want
+
+
+@pytest.mark.parametrize("precision", ["bf16x3", "fp32"])
+def test_rbf16k_all_probes_match_oracle(rbf16k, precision):
+    x, key, k, p, want = rbf16k
+    n = x.shape[0]
+    op = mf.RBFKernelOperator(_t(x, torch.float32), precision=precision)
+    sampler = mf.stochtrace.sampler_signs(torch.ones(n, device=DEV), num=p)
+    integrand = mf.funm.monte_carlo_funm_sym_logdet(mf.decomp.tridiag_sym(k))
+    got = mf.stochtrace.estimator_monte_carlo(integrand, sampler)(op, key)
+    assert _rel(got, want.mean()) <= 1e-4, (float(got), want.mean())
+    per = integrand.batched(op, sampler(key)).cpu().numpy()
+    assert _rel(per.mean(), float(got)) <= 1e-12
+    # no probe is far off: the per-probe values carry the same errors
+    assert np.max(np.abs(per - want) / np.abs(want)) <= 2e-3
+
+
+# ---------------------------------------------------------------- laplace1m
+
+
+def test_laplace1m_full_size_probe_subset_matches_oracle():
+    m, k, p, num = 1024, 100, 64, 4
+    L = problems.laplacian_2d(m, shift=0.1)
+    op = mf.CSROperator.from_scipy(L)
+    key = mf.prng.prng_key(1)
+    sampler = mf.stochtrace.sampler_signs(torch.ones(m * m, device=DEV), num=p)
+    integrand = mf.funm.monte_carlo_funm_sym_logdet(mf.decomp.tridiag_sym(k))
+    got = integrand.batched(op, sampler(key)).cpu().numpy()
+    assert got.shape == (p,) and np.all(np.isfinite(got))
+    V = philox.rademacher(np.asarray(key, np.uint32), num, m * m)
+    L64 = L.astype(np.float64)
+    want = slq.slq_batched(lambda X: (L64 @ X.T).T, k, V)
+    np.testing.assert_allclose(got[:num], want, rtol=1e-4)
+
+
+# ------------------------------------------------------------------- grad8k
+
+
+@pytest.fixture(scope="module")
+def grad8k():
+    n, k, p = 8192, 48, 128
+    x = np.random.default_rng(0).uniform(0.0, 1.0, size=(n, 3)).astype(np.float32)
+    theta0 = np.array([0.0, math.log(0.2), math.log(1e-2)])
+    key = mf.prng.prng_key(1)
+    V = philox.rademacher(np.asarray(key, np.uint32), p, n)
+    matmat, vjp_matmat = oadj.rbf_vjp_factory(x.astype(np.float64), theta0)
+    val, grad = oadj.slq_grad_batched(matmat, vjp_matmat, 3, k, V)
+    del matmat, vjp_matmat
+    h = 1e-4
+    fd = np.zeros(3)
+    for i in range(3):
+        vals = []
+        for sgn in (1.0, -1.0):
+            th = theta0.copy()
+            th[i] += sgn * h
+            s2, ell, tau = np.exp(th)
+            K = problems.rbf_kernel(x.astype(np.float64), s2, ell, tau)
+            vals.append(slq.slq_batched(lambda X: X @ K, k, V).mean())
+            del K
+        fd[i] = (vals[0] - vals[1]) / (2 * h)
+    return x, theta0, V, k, val, grad, fd
+
+
+def test_grad8k_oracle_adjoint_matches_central_differences(grad8k):
+    *_, grad, fd = grad8k
+    np.testing.assert_allclose(grad, fd, rtol=1e-6)
+
+
+@pytest.mark.parametrize("precision,tol_val,tol_grad", [("fp64", 1e-9, 1e-8), ("bf16x3", 1e-4, 3e-3)])
+def test_grad8k_gpu_gradient_matches_oracle(grad8k, precision, tol_val, tol_grad):
+    x, theta0, V, k, val, grad, fd = grad8k
+    dt = torch.float64 if precision == "fp64" else torch.float32
+    theta = torch.tensor(theta0, dtype=torch.float64, requires_grad=True)
+    got = autodiff.rbf_logdet(_t(x, torch.float32), theta, _t(V, dt), k, precision=precision)
+    got.backward()
+    assert _rel(got.detach(), val) <= tol_val
+    g = theta.grad.numpy()
+    np.testing.assert_allclose(g, grad, rtol=tol_grad)
+    np.testing.assert_allclose(g, fd, rtol=tol_grad + 1e-6)
+
+
+# -------------------------------------------------------------------- serve
+
+
+def test_serving_stream_requests_match_oracle():
+    # requests of the seeded benchmark stream (rate 150/s, seed 0): the three
+    # largest whose float64 solve stays under 6e12 flop, and the smallest one
+    stream = serve.synthetic_stream(300, rate=150.0, seed=0)
+    cost = {r.rid: 2.0 * r.x.shape[0] ** 2 * r.p * r.k for r in stream}
+    big = sorted((r for r in stream if cost[r.rid] <= 6e12), key=lambda r: -r.x.shape[0])[:3]
+    small = min(stream, key=lambda r: r.x.shape[0])
+    chosen = big + [small]
+    for r in chosen:
+        r.arrival = 0.0
+    assert max(r.x.shape[0] for r in chosen) > 32000
+    results, stats = serve.SLQServer(slots=4).run(chosen, realtime=False)
+    assert stats["solves"] == len(chosen)
+    by_id = {res.rid: res for res in results}
+    for r in chosen:
+        n = r.x.shape[0]
+        K = problems.rbf_kernel(r.x.astype(np.float64), r.s2, r.ell, r.tau)
+        V = philox.rademacher(np.asarray(r.key, np.uint32), r.p, n)
+        f = np.log if r.fun == "log" else (lambda t, s=float(r.fun.split(":")[1]): np.exp(s * t))
+        want = slq.slq_batched(lambda X: X @ K, r.k, V, matfun=f)
+        del K
+        assert _rel(by_id[r.rid].mean, want.mean()) <= 1e-4, (r.rid, n, r.k, r.p, r.fun)

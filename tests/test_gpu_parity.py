@@ -356,3 +356,44 @@ def test_slq_rbf_precisions_vs_fp64(precision, tol):
         K = problems.rbf_kernel(x.astype(np.float64))
     want = slq.slq_batched(lambda X: X @ K, k, V).mean()
     assert abs(got - want) <= tol * abs(want), (got, want, abs(got - want) / abs(want))
+
+
+# ------------------------------------------------------------ DLPack intake
+
+
+class _DLPackOnly:
+    """A CUDA array that exports its memory only through the DLPack protocol
+    (as CuPy, JAX or Numba arrays do)."""
+
+    def __init__(self, t):
+        self._t = t
+
+    def __dlpack__(self, stream=None, **kwargs):
+        return self._t.__dlpack__(stream=stream) if stream is not None else self._t.__dlpack__()
+
+    def __dlpack_device__(self):
+        return self._t.__dlpack_device__()
+
+
+def test_dlpack_inputs_give_the_torch_results():
+    n, k, p = 700, 20, 12
+    A = problems.dense_spd(n, seed=5)
+    At = _t(A, torch.float32)
+    V = _t(np.random.default_rng(3).standard_normal((p, n)), torch.float32)
+    integrand = mf.funm.monte_carlo_funm_sym_logdet(mf.decomp.tridiag_sym(k))
+    want = integrand.batched(mf.DenseOperator(At), V)
+    op = mf.DenseOperator(_DLPackOnly(At))
+    got = integrand.batched(op, _DLPackOnly(V))
+    torch.testing.assert_close(got, want, rtol=0, atol=0)
+    got2 = integrand.batched(op, torch.utils.dlpack.to_dlpack(V))
+    torch.testing.assert_close(got2, want, rtol=0, atol=0)
+    # the sampler's x_like and the RBF points may be DLPack producers as well
+    s = mf.stochtrace.sampler_signs(_DLPackOnly(torch.ones(n, device=DEV)), num=p)
+    key = mf.prng.prng_key(3)
+    est = mf.stochtrace.estimator_monte_carlo(integrand, s)(op, key)
+    np.testing.assert_allclose(float(est), float(integrand.batched(mf.DenseOperator(At), s(key)).mean()),
+                               rtol=0, atol=0)
+    x = _t(problems.rbf_points(300, seed=1), torch.float32)
+    a = mf.RBFKernelOperator(_DLPackOnly(x), precision="fp32").dense()
+    b = mf.RBFKernelOperator(x, precision="fp32").dense()
+    assert torch.equal(a, b)

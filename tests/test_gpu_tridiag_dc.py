@@ -130,7 +130,7 @@ def test_log_quadrature_of_lanczos_tridiagonals(k):
         assert abs(got[b] - want) <= 1e-10 * max(abs(want), 1.0)
 
 
-@pytest.mark.parametrize("k", [1, 2, 17, 48, 100])
+@pytest.mark.parametrize("k", [1, 2, 15, 16, 17, 32, 48, 64, 65, 100])
 def test_tridiag_eigh_full_vectors(k):
     # mfg_tridiag_eigh: every eigenvector (the derivative of e1^T f(T) e1 uses them)
     rng = np.random.default_rng(2000 + k)

@@ -191,3 +191,41 @@ def test_eigh_and_adjoint_argument_errors_without_gpu():
     assert lib.mfg_hessenberg_adjoint(ctypes.byref(A), 4, 1, 16, *bad) == _lib.MFG_ERR_BAD_ARG
     small_ws = args[:-2] + (16, None)
     assert lib.mfg_hessenberg_adjoint(ctypes.byref(A), 4, 1, 16, *small_ws) == _lib.MFG_ERR_WORKSPACE
+
+
+# ------------------------------------------------------------ DLPack intake
+
+
+class _DLPackOnly:
+    """An array that exports its memory only through the DLPack protocol."""
+
+    def __init__(self, t):
+        self._t = t
+
+    def __dlpack__(self, stream=None, **kwargs):
+        return self._t.__dlpack__()
+
+    def __dlpack_device__(self):
+        return self._t.__dlpack_device__()
+
+
+def test_dlpack_producers_are_imported_without_copy():
+    import torch
+
+    from matfree_gb300._panel import as_tensor
+
+    t = torch.arange(6.0)
+    for obj in (_DLPackOnly(t), torch.utils.dlpack.to_dlpack(t), np.arange(6.0)):
+        got = as_tensor(obj, "x")
+        assert isinstance(got, torch.Tensor)
+        np.testing.assert_array_equal(got.numpy(), np.arange(6.0))
+    assert as_tensor(_DLPackOnly(t), "x").data_ptr() == t.data_ptr()
+
+
+def test_host_arrays_and_unknown_objects_are_rejected():
+    from matfree_gb300._panel import require_cuda
+
+    with pytest.raises(TypeError, match="CUDA"):
+        require_cuda(np.zeros(3), "x")  # a DLPack producer, but host memory
+    with pytest.raises(TypeError, match="DLPack"):
+        require_cuda([1.0, 2.0], "x")
