@@ -161,6 +161,25 @@ MFG_API int mfg_hessenberg_adjoint(const mfg_operator *op, int64_t k, int64_t p,
                                    const double *dc, void *Lambda, void *dv, void *workspace,
                                    size_t workspace_bytes, void *stream);
 
+/* mfg_hessenberg_adjoint with a cotangent of the basis as well: dQ (p*k
+ * rows of ld, layout of Q; NULL means zero) enters through Pi_xi = dQ^T +
+ * gamma r^T and Pi_gamma = ... - dQ^T Q (matfree/decomp.py:505-506, used by
+ * the reverse step at :592-599).  Every integrand that reads Q -- f(A) v by
+ * Lanczos (funm.py:114-147) -- needs it.  Same workspace and outputs as
+ * mfg_hessenberg_adjoint, which is this call with dQ = NULL. */
+MFG_API int mfg_hessenberg_adjoint_ex(const mfg_operator *op, int64_t k, int64_t p, int64_t ld,
+                                      const void *Q, const double *H, const void *residual,
+                                      const double *init_len_inv, const void *dQ, const double *dH,
+                                      const void *dr, const double *dc, void *Lambda, void *dv,
+                                      void *workspace, size_t workspace_bytes, void *stream);
+
+/* out_b = sum_i coef[b][i] q_{b,i} for p Krylov bases Q (p*k rows of ld,
+ * dtype MFG_F32/MFG_F64; coef p x k float64): the back-projection
+ * Q^T (f(T) e1) of f(A) v by Lanczos (matfree/funm.py:142-146), batched.
+ * Columns n..ld-1 of out are set to zero. */
+MFG_API int mfg_basis_combine(int32_t dtype, int64_t k, int64_t p, int64_t n, int64_t ld,
+                              const void *Q, const double *coef, void *out, void *stream);
+
 /* Eigenvalues (ascending, eigvals p x k) and every eigenvector (eigvecs p
  * k x k, row-major, column j = eigenvector j) of the symmetric tridiagonal
  * part of (H + H^T)/2 for p Hessenberg matrices, in float64: divide and

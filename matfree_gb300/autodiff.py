@@ -67,8 +67,9 @@ def quadform_dH(H: torch.Tensor, scale: torch.Tensor, f, fprime) -> tuple[torch.
     return values, dH
 
 
-def hessenberg_adjoint(op, Q, H, R, c, dH, dr=None, dc=None):
-    """GPU reverse pass.  Q (p, k, ld) / R (p, ld) are the forward panels.
+def hessenberg_adjoint(op, Q, H, R, c, dH, dr=None, dc=None, dQ=None):
+    """GPU reverse pass.  Q (p, k, ld) / R (p, ld) are the forward panels;
+    dQ (p, k, ld) and dr (p, ld) are optional cotangents in the same layout.
 
     Returns (Lambda (p, k, ld), dv (p, ld)).
     """
@@ -83,10 +84,14 @@ def hessenberg_adjoint(op, Q, H, R, c, dH, dr=None, dc=None):
     nbytes = lib.mfg_adjoint_workspace_bytes(ctypes.byref(s), k, p, ld)
     ws, wsb = _WS.get(nbytes, Q.device)
     vp = lambda t: ctypes.c_void_p(t.data_ptr()) if t is not None else ctypes.c_void_p(0)  # noqa: E731
-    st = lib.mfg_hessenberg_adjoint(ctypes.byref(s), k, p, ld, vp(Q), vp(H.contiguous()), vp(R), vp(c),
-                                    vp(dH.contiguous()), vp(dr), vp(dc), vp(Lam), vp(dv), ws, wsb,
-                                    stream_ptr())
-    _lib.check(st, "mfg_hessenberg_adjoint")
+    st = lib.mfg_hessenberg_adjoint_ex(ctypes.byref(s), k, p, ld, vp(Q), vp(H.contiguous()), vp(R), vp(c),
+                                       vp(dQ), vp(dH.contiguous()), vp(dr), vp(dc), vp(Lam), vp(dv), ws,
+                                       wsb, stream_ptr())
+    err = getattr(op, "error", None)
+    if err is not None:  # a callback operator raised inside the reverse sweep
+        op.error = None
+        raise err
+    _lib.check(st, "mfg_hessenberg_adjoint_ex")
     return Lam, dv
 
 
@@ -288,6 +293,187 @@ class _CallbackQuadform(torch.autograd.Function):
         return (None, None, *grads)
 
 
+def _params_vjp(fn, batched, params_tree, leaves, want, Qf, Lf):
+    """sum_j Lf_j^T d(A(params) Qf_j)/d params for the leaves listed in want
+    (one autograd VJP of the matvec over all stacked basis vectors)."""
+    grads = [None] * len(leaves)
+    if not want:
+        return grads
+    n = Qf.shape[1]
+    with torch.enable_grad():
+        live = [t.detach().requires_grad_(True) if i in want else t for i, t in enumerate(leaves)]
+        params = _rebuild(params_tree, iter(live))
+        AQ = CallbackOperator(fn, n, dtype=Qf.dtype, batched=batched, params=params)._apply_rows(Qf)
+        total = (Lf.to(AQ.dtype) * AQ).sum()
+        gs = torch.autograd.grad(total, [live[i] for i in want], allow_unused=True)
+    for i, g in zip(want, gs):
+        grads[i] = torch.zeros_like(leaves[i]) if g is None else g.to(leaves[i].dtype)
+    return grads
+
+
+class _ArnoldiFull(torch.autograd.Function):
+    """Batched Arnoldi with full reorthogonalisation whose backward pass is the
+    Hessenberg adjoint: the custom VJP that matfree puts on the decomposition
+    (matfree/decomp.py:393-422).
+
+    Inputs: the starting vectors V (p, n) and the tensor leaves of the matvec's
+    parameters.  Outputs: Q (p, k, n), H (p, k, k) float64, residual (p, n)
+    and 1/||v|| (p,) float64, as ``run_hessenberg``.  The backward pass takes
+    the cotangents of all four (dQ, dH, dr, dc; absent ones are zero), runs
+    ``mfg_hessenberg_adjoint_ex`` on the GPU and returns dV = lambda c and the
+    parameter gradient sum_{b,j} lambda_bj^T d(A q_bj)/d params.
+    """
+
+    @staticmethod
+    def forward(ctx, spec, V, *leaves):
+        op_fixed, fn, n, k, batched, params_tree = spec
+        if op_fixed is not None:
+            op = op_fixed
+        else:
+            params = _rebuild(params_tree, iter(leaves))
+            op = CallbackOperator(fn, n, dtype=V.dtype, batched=batched, params=params)
+        panel, ld = as_panel(V.detach(), n, op.basis_dtype)
+        Q, H, R, c = _forward_panels(op, k, panel, ld)
+        ctx.save_for_backward(Q, H, R, c)
+        ctx.op, ctx.spec, ctx.leaves = op, spec, leaves
+        return Q[:, :, :n], H, R[:, :n], c
+
+    @staticmethod
+    def backward(ctx, dQ, dH, dR, dc):
+        Q, H, R, c = ctx.saved_tensors
+        op_fixed, fn, n, k, batched, params_tree = ctx.spec
+        p, _, ld = Q.shape
+        leaves = ctx.leaves
+        want = [i for i in range(len(leaves)) if ctx.needs_input_grad[2 + i]]
+        if not ctx.needs_input_grad[1] and not want:
+            return (None, None, *([None] * len(leaves)))
+        dQp = None
+        if dQ is not None:
+            dQp = torch.zeros_like(Q)
+            dQp[:, :, :n] = dQ.to(Q.dtype)
+        dRp = None
+        if dR is not None:
+            dRp = torch.zeros_like(R)
+            dRp[:, :n] = dR.to(R.dtype)
+        dH = torch.zeros_like(H) if dH is None else dH.to(torch.float64).contiguous()
+        dc = None if dc is None else dc.to(torch.float64).contiguous()
+        Lam, dv = hessenberg_adjoint(ctx.op, Q, H, R, c, dH, dr=dRp, dc=dc, dQ=dQp)
+        dV = dv[:, :n] if ctx.needs_input_grad[1] else None
+        grads = [None] * len(leaves)
+        if want and op_fixed is None:
+            grads = _params_vjp(fn, batched, params_tree, leaves, want,
+                                Q[:, :, :n].reshape(p * k, n), Lam[:, :, :n].reshape(p * k, n))
+        return (None, dV, *grads)
+
+
+def arnoldi_full(op, k: int, V: torch.Tensor):
+    """Differentiable batched Arnoldi (full reorthogonalisation) of the rows of V.
+
+    ``op`` is an operator descriptor (gradients flow to V only) or a
+    ``CallbackOperator`` (gradients also flow to the tensor leaves of its
+    parameters).  Returns (Q (p, k, n), H (p, k, k), residual (p, n), 1/||v|| (p,)).
+    """
+    if k <= 0:
+        # decomp.py:483-486
+        raise ValueError("Custom Hessenberg-adjoints are not implemented for num_matvecs = 0.")
+    if isinstance(op, CallbackOperator):
+        spec = (None, op.fn, int(op.n), int(k), op.batched, tuple(op.params))
+        leaves = tree_leaves(tuple(op.params))
+    else:
+        spec = (op, None, int(op.n), int(k), False, ())
+        leaves = []
+    return _ArnoldiFull.apply(spec, V, *leaves)
+
+
+def wants_grad(V, op) -> bool:
+    """Whether the decomposition of V under op must be differentiable."""
+    if not torch.is_grad_enabled():
+        return False
+    if isinstance(V, torch.Tensor) and V.requires_grad:
+        return True
+    return isinstance(op, CallbackOperator) and params_require_grad(op.params)
+
+
+class _FunmE1(torch.autograd.Function):
+    """f(T) e1 (p, k) for a stack of symmetric tridiagonal T (p, k, k) float64,
+    through the device eigensolver (mfg_tridiag_eigh); the backward pass is the
+    Daleckii-Krein formula dL/dT = S (F o (S^T dy)(S^T e1)^T) S^T, with F the
+    divided differences of f at the eigenvalues (f' on the diagonal) -- what
+    autodiff through eigh computes for matfree's dense_funm_sym_eigh
+    (matfree/funm.py:322-335)."""
+
+    @staticmethod
+    def forward(ctx, T, f, fprime):
+        from .funm import tridiag_eigh
+
+        w, S = tridiag_eigh(T.detach().contiguous())
+        fw = f(w)
+        s1 = S[:, 0, :]
+        y = torch.einsum("pij,pj->pi", S, fw * s1)
+        ctx.save_for_backward(w, S)
+        ctx.fun = (f, fprime)
+        return y
+
+    @staticmethod
+    def backward(ctx, dy):
+        w, S = ctx.saved_tensors
+        f, fprime = ctx.fun
+        fw = f(w)
+        diff = w[:, :, None] - w[:, None, :]
+        same = diff.abs() <= 1e-13 * torch.clamp(w.abs()[:, :, None], min=1.0)
+        F = (fw[:, :, None] - fw[:, None, :]) / torch.where(same, torch.ones_like(diff), diff)
+        F = torch.where(same, fprime(0.5 * (w[:, :, None] + w[:, None, :])), F)
+        u = torch.einsum("pji,pj->pi", S, dy.to(torch.float64))
+        v = S[:, 0, :]
+        G = S @ (F * u[:, :, None] * v[:, None, :]) @ S.transpose(-1, -2)
+        return G, None, None
+
+
+def funm_e1(T: torch.Tensor, dense_funm) -> torch.Tensor:
+    """Differentiable f(T) e1 for a stack of symmetric tridiagonal matrices."""
+    f, fprime = _fun_pair(dense_funm)
+    return _FunmE1.apply(T.to(torch.float64), f, fprime)
+
+
+class _BasisCombine(torch.autograd.Function):
+    """y_b = sum_i coef[b, i] q_{b,i} (the back-projection of funm.py:142-146) on
+    the device (mfg_basis_combine); backward: dcoef = Q dy, dQ = coef dy^T."""
+
+    @staticmethod
+    def forward(ctx, Q, coef):
+        p, k, n = Q.shape
+        ld = Q.stride(1) if k > 1 else padded_ld(n)
+        base = Q
+        if Q.stride(2) != 1 or ld % 8 or ld < n or Q.data_ptr() % 16 or (p > 1 and Q.stride(0) != k * ld):
+            base = torch.zeros((p, k, padded_ld(n)), dtype=Q.dtype, device=Q.device)
+            base[:, :, :n] = Q
+            ld = base.shape[2]
+        out = torch.zeros((p, ld), dtype=Q.dtype, device=Q.device)
+        cf = coef.to(torch.float64).contiguous()
+        dt = _lib.MFG_F64 if Q.dtype == torch.float64 else _lib.MFG_F32
+        st = _lib.lib().mfg_basis_combine(dt, k, p, n, ld, ctypes.c_void_p(base.data_ptr()),
+                                          ctypes.c_void_p(cf.data_ptr()), ctypes.c_void_p(out.data_ptr()),
+                                          stream_ptr())
+        _lib.check(st, "mfg_basis_combine")
+        ctx.save_for_backward(Q, coef)
+        return out[:, :n]
+
+    @staticmethod
+    def backward(ctx, dy):
+        Q, coef = ctx.saved_tensors
+        dQ = dcoef = None
+        if ctx.needs_input_grad[0]:
+            dQ = coef.to(Q.dtype)[:, :, None] * dy.to(Q.dtype)[:, None, :]
+        if ctx.needs_input_grad[1]:
+            dcoef = torch.einsum("pkn,pn->pk", Q.double(), dy.double()).to(coef.dtype)
+        return dQ, dcoef
+
+
+def basis_combine(Q: torch.Tensor, coef: torch.Tensor) -> torch.Tensor:
+    """Differentiable sum_i coef[b, i] Q[b, i, :] on the device."""
+    return _BasisCombine.apply(Q, coef)
+
+
 def callback_quadform(fn, n: int, k: int, samples: torch.Tensor, dense_funm, params=(),
                       batched: bool = False) -> torch.Tensor:
     """Differentiable integrand values (p,) float64 for a callable matvec
@@ -301,4 +487,5 @@ def callback_quadform(fn, n: int, k: int, samples: torch.Tensor, dense_funm, par
 
 
 __all__ = ["quadform_dH", "hessenberg_adjoint", "rbf_logdet", "rbf_theta_contractions",
-           "run_hessenberg", "callback_quadform", "params_require_grad"]
+           "run_hessenberg", "callback_quadform", "params_require_grad", "arnoldi_full", "wants_grad",
+           "funm_e1", "basis_combine"]

@@ -82,17 +82,54 @@ __global__ void adj_step_coef_kernel(const double *__restrict__ H, const double 
   }
 }
 
-// out[b][r] = U[b][r] - alpha_b lam[b][r] + gam_b R[b][r]
+// out[b][r] = U[b][r] - alpha_b lam[b][r] + gam_b R[b][r] (+ dq[b][r] when the
+// cotangent of the basis is given: its column idx, dq_bstride apart per probe)
 template <typename T>
 __global__ void adj_lincomb_kernel(const T *__restrict__ U, const T *__restrict__ lam,
-                                   const T *__restrict__ R, const double *__restrict__ scal,
-                                   int64_t n, int64_t ld, int64_t p, T *__restrict__ out) {
+                                   const T *__restrict__ R, const T *__restrict__ dq, int64_t dq_bstride,
+                                   const double *__restrict__ scal, int64_t n, int64_t ld, int64_t p,
+                                   T *__restrict__ out) {
   const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t b = blockIdx.y;
   if (r >= n || b >= p) return;
   const T alpha = (T)scal[b * 3 + 0], gam = (T)scal[b * 3 + 1];
   const int64_t o = b * ld + r;
-  out[o] = U[o] - alpha * lam[o] + gam * R[o];
+  T v = U[o] - alpha * lam[o] + gam * R[o];
+  if (dq) v += dq[b * dq_bstride + r];
+  out[o] = v;
+}
+
+// y[i] += a x[i] (float64)
+__global__ void axpy_f64_kernel(double a, const double *__restrict__ x, double *__restrict__ y,
+                                int64_t m) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < m) y[i] += a * x[i];
+}
+
+// out[b][r] = sum_i coef[b][i] Q[b][i][r] for r < n, 0 for n <= r < ld: the
+// back-projection Q^T (f(T) e1) of a batch of Krylov bases (p, k, ld).  The
+// coefficients are staged in shared memory kCombineCoef at a time; each
+// thread owns one row and sums over i in a fixed order.
+constexpr int kCombineCoef = 512;
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+basis_combine_kernel(const T *__restrict__ Q, int64_t k, int64_t ld, int64_t n,
+                     const double *__restrict__ coef, T *__restrict__ out) {
+  __shared__ T sc[kCombineCoef];
+  const int64_t b = blockIdx.y;
+  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const T *Qb = Q + b * k * ld;
+  T acc = 0;
+  for (int64_t i0 = 0; i0 < k; i0 += kCombineCoef) {
+    const int m = (int)(k - i0 < kCombineCoef ? k - i0 : kCombineCoef);
+    __syncthreads();
+    for (int t = threadIdx.x; t < m; t += blockDim.x) sc[t] = (T)coef[b * k + i0 + t];
+    __syncthreads();
+    if (r < n)
+      for (int t = 0; t < m; ++t) acc += sc[t] * Qb[(i0 + t) * ld + r];
+  }
+  if (r < ld) out[b * ld + r] = r < n ? acc : (T)0;
 }
 
 // beta[b] = scal[b][2] (the divisor of step idx), for the normalise kernel
@@ -131,15 +168,37 @@ int launch_adj_step_coef(const double *H, const double *Pi, const double *g, con
 }
 
 template <typename T>
-int launch_adj_lincomb(const T *U, const T *lam, const T *R, const double *scal, int64_t n,
-                       int64_t ld, int64_t p, T *out, cudaStream_t s) {
+int launch_adj_lincomb(const T *U, const T *lam, const T *R, const T *dq, int64_t dq_bstride,
+                       const double *scal, int64_t n, int64_t ld, int64_t p, T *out, cudaStream_t s) {
   if (p > 65535) return MFG_ERR_UNSUPPORTED;
-  adj_lincomb_kernel<T><<<dim3(blocks(n, 256), (unsigned)p), 256, 0, s>>>(U, lam, R, scal, n, ld, p, out);
+  adj_lincomb_kernel<T><<<dim3(blocks(n, 256), (unsigned)p), 256, 0, s>>>(U, lam, R, dq, dq_bstride, scal,
+                                                                          n, ld, p, out);
   return MFG_LAUNCH_STATUS();
 }
-template int launch_adj_lincomb<float>(const float *, const float *, const float *, const double *,
-                                       int64_t, int64_t, int64_t, float *, cudaStream_t);
+template int launch_adj_lincomb<float>(const float *, const float *, const float *, const float *,
+                                       int64_t, const double *, int64_t, int64_t, int64_t, float *,
+                                       cudaStream_t);
 template int launch_adj_lincomb<double>(const double *, const double *, const double *, const double *,
-                                        int64_t, int64_t, int64_t, double *, cudaStream_t);
+                                        int64_t, const double *, int64_t, int64_t, int64_t, double *,
+                                        cudaStream_t);
+
+template <typename T>
+int launch_basis_combine(const T *Q, int64_t k, int64_t ld, int64_t n, int64_t p, const double *coef,
+                         T *out, cudaStream_t s) {
+  if (p <= 0) return MFG_OK;
+  if (p > 65535) return MFG_ERR_UNSUPPORTED;
+  basis_combine_kernel<T><<<dim3(blocks(ld, 256), (unsigned)p), 256, 0, s>>>(Q, k, ld, n, coef, out);
+  return MFG_LAUNCH_STATUS();
+}
+template int launch_basis_combine<float>(const float *, int64_t, int64_t, int64_t, int64_t,
+                                         const double *, float *, cudaStream_t);
+template int launch_basis_combine<double>(const double *, int64_t, int64_t, int64_t, int64_t,
+                                          const double *, double *, cudaStream_t);
+
+int launch_axpy_f64(double a, const double *x, double *y, int64_t m, cudaStream_t s) {
+  if (m <= 0) return MFG_OK;
+  axpy_f64_kernel<<<blocks(m, 256), 256, 0, s>>>(a, x, y, m);
+  return MFG_LAUNCH_STATUS();
+}
 
 }  // namespace mfg

@@ -448,7 +448,7 @@ static int run_hessenberg(const mfg_operator *op, int64_t k, int64_t p, const T 
 // ---------------------------------------------------------------------------
 
 struct AdjLayout {
-  size_t lam, lam2, U, panel, h, g, coef, bp, gamma, scal, beta, Gamma, Pi, inv, partials,
+  size_t lam, lam2, U, panel, h, g, coef, bp, gamma, scal, beta, Gamma, Pi, M, inv, partials,
       counters, status, hi, lo, total;
 };
 
@@ -476,6 +476,7 @@ static AdjLayout adj_layout(const mfg_operator *op, int64_t k, int64_t p, int64_
   L.beta = take((size_t)p * 8);
   L.Gamma = take((size_t)p * kk * kk * 8);
   L.Pi = take((size_t)p * kk * kk * 8);
+  L.M = take((size_t)p * kk * kk * 8);
   L.inv = take((size_t)p * 8);
   L.partials = take((size_t)p * nch * (kk + 1) * 8);
   L.counters = take((size_t)p * 4);
@@ -488,8 +489,8 @@ static AdjLayout adj_layout(const mfg_operator *op, int64_t k, int64_t p, int64_
 
 template <typename T>
 static int run_adjoint(const mfg_operator *op, int64_t k, int64_t p, int64_t ld, const T *Q,
-                       const double *H, const T *R, const double *c, const double *dH, const T *dr,
-                       const double *dc, T *Lam, T *dv, const AdjLayout &L, char *ws,
+                       const double *H, const T *R, const double *c, const T *dQ, const double *dH,
+                       const T *dr, const double *dc, T *Lam, T *dv, const AdjLayout &L, char *ws,
                        cudaStream_t s) {
   const int64_t n = op->n;
   const int64_t qb = k * ld;
@@ -524,6 +525,16 @@ static int run_adjoint(const mfg_operator *op, int64_t k, int64_t p, int64_t ld,
   MFG_CUDA_TRY(cudaMemsetAsync(lam, 0, (size_t)p * ld * sizeof(T), s));
   MFG_LAUNCH(MFG_PROF_OTHER, 24.0 * p * k * k, 2.0 * p * k * k * k,
              launch_pi_gamma(H, dH, dc, c, (int)k, p, Pi, s));
+  if (dQ) {
+    // Pi_gamma -= dQ^T Q   (decomp.py:506): row i of M is Q^T dq_i, one sweep per column of dQ
+    double *M = reinterpret_cast<double *>(ws + L.M);
+    for (int64_t i = 0; i < k; ++i)
+      MFG_LAUNCH(MFG_PROF_PROJ, (k + 1.0) * vecb, 2.0 * k * vecb / sizeof(T),
+                 launch_proj<T>(Q, qb, ld, (int)k, dQ + i * ld, qb, n, p, partials, counters, M + i * k,
+                                k * k, 1, s, status));
+    MFG_LAUNCH(MFG_PROF_OTHER, 24.0 * p * k * k, (double)p * k * k,
+               launch_axpy_f64(-1.0, M, Pi, p * k * k, s));
+  }
   // gamma = dH e_K - Q^T dr ;  lambda = dr + Q gamma   (decomp.py:498-499)
   if (dr) {
     MFG_LAUNCH(MFG_PROF_PROJ, (k + 1.0) * vecb, 2.0 * k * vecb / sizeof(T),
@@ -559,8 +570,10 @@ static int run_adjoint(const mfg_operator *op, int64_t k, int64_t p, int64_t ld,
     MFG_CUDA_TRY(cudaMemcpy2DAsync(Lam + idx * ld, qb * sizeof(T), lam, ld * sizeof(T),
                                    ld * sizeof(T), p, cudaMemcpyDeviceToDevice, s));
     // lambda = (gamma_idx r + Q G - alpha lambda + U - Lambda beta_plus) / beta_minus
-    MFG_LAUNCH(MFG_PROF_SCALE, 4.0 * vecb, 3.0 * vecb / sizeof(T),
-               launch_adj_lincomb<T>(U, lam, R, scal, n, ld, p, lam2, s));
+    // Pi_xi row idx = dq_idx + gamma_idx r   (decomp.py:505)
+    MFG_LAUNCH(MFG_PROF_SCALE, (dQ ? 5.0 : 4.0) * vecb, (dQ ? 4.0 : 3.0) * vecb / sizeof(T),
+               launch_adj_lincomb<T>(U, lam, R, dQ ? dQ + idx * ld : nullptr, qb, scal, n, ld, p, lam2,
+                                     s));
     MFG_LAUNCH(MFG_PROF_SUB, (k + 2.0) * vecb, 2.0 * k * vecb / sizeof(T),
                launch_sub<T>(Q, qb, ld, (int)k, coef, k, 1, lam2, lam2, ld, n, p, false, true,
                              partials, counters, nullptr, nullptr, 0, s, status));
@@ -1115,17 +1128,18 @@ size_t mfg_adjoint_workspace_bytes(const mfg_operator *op, int64_t k, int64_t p,
   return adj_layout(op, k, p, ld).total;
 }
 
-int mfg_hessenberg_adjoint(const mfg_operator *op, int64_t k, int64_t p, int64_t ld, const void *Q,
-                           const double *H, const void *residual, const double *init_len_inv,
-                           const double *dH, const void *dr, const double *dc, void *Lambda,
-                           void *dv, void *workspace, size_t workspace_bytes, void *stream) {
+int mfg_hessenberg_adjoint_ex(const mfg_operator *op, int64_t k, int64_t p, int64_t ld, const void *Q,
+                              const double *H, const void *residual, const double *init_len_inv,
+                              const void *dQ, const double *dH, const void *dr, const double *dc,
+                              void *Lambda, void *dv, void *workspace, size_t workspace_bytes,
+                              void *stream) {
   MFG_TRY(check_op(op));
   MFG_TRY(check_panel(op, p, ld));
   if (k == 0) return MFG_ERR_RANGE;  // decomp.py:483-486: not defined for num_matvecs = 0
   if (k < 0 || k > op->n) return MFG_ERR_RANGE;
   if (!Q || !H || !residual || !init_len_inv || !dH || !Lambda || !dv) return MFG_ERR_BAD_ARG;
   if (!aligned16(Q) || !aligned16(residual) || !aligned16(Lambda) || !aligned16(dv) ||
-      (dr && !aligned16(dr)))
+      (dr && !aligned16(dr)) || (dQ && !aligned16(dQ)))
     return MFG_ERR_BAD_ARG;
   const AdjLayout L = adj_layout(op, k, p, ld);
   if (!workspace || workspace_bytes < L.total) return MFG_ERR_WORKSPACE;
@@ -1133,10 +1147,36 @@ int mfg_hessenberg_adjoint(const mfg_operator *op, int64_t k, int64_t p, int64_t
   cudaStream_t s = as_stream(stream);
   if (op->precision == MFG_PREC_FP64)
     return run_adjoint<double>(op, k, p, ld, (const double *)Q, H, (const double *)residual,
-                               init_len_inv, dH, (const double *)dr, dc, (double *)Lambda,
-                               (double *)dv, L, ws, s);
+                               init_len_inv, (const double *)dQ, dH, (const double *)dr, dc,
+                               (double *)Lambda, (double *)dv, L, ws, s);
   return run_adjoint<float>(op, k, p, ld, (const float *)Q, H, (const float *)residual, init_len_inv,
-                            dH, (const float *)dr, dc, (float *)Lambda, (float *)dv, L, ws, s);
+                            (const float *)dQ, dH, (const float *)dr, dc, (float *)Lambda, (float *)dv,
+                            L, ws, s);
+}
+
+int mfg_hessenberg_adjoint(const mfg_operator *op, int64_t k, int64_t p, int64_t ld, const void *Q,
+                           const double *H, const void *residual, const double *init_len_inv,
+                           const double *dH, const void *dr, const double *dc, void *Lambda,
+                           void *dv, void *workspace, size_t workspace_bytes, void *stream) {
+  return mfg_hessenberg_adjoint_ex(op, k, p, ld, Q, H, residual, init_len_inv, nullptr, dH, dr, dc,
+                                   Lambda, dv, workspace, workspace_bytes, stream);
+}
+
+int mfg_basis_combine(int32_t dtype, int64_t k, int64_t p, int64_t n, int64_t ld, const void *Q,
+                      const double *coef, void *out, void *stream) {
+  if (k < 0 || p < 0 || n <= 0 || ld < n || ld % 8 != 0) return MFG_ERR_BAD_ARG;
+  if (dtype != MFG_F32 && dtype != MFG_F64) return MFG_ERR_BAD_ARG;
+  if (p == 0) return MFG_OK;
+  if ((k > 0 && (!Q || !coef)) || !out || !aligned16(out) || (Q && !aligned16(Q))) return MFG_ERR_BAD_ARG;
+  cudaStream_t s = as_stream(stream);
+  const double es = dtype == MFG_F64 ? 8.0 : 4.0;
+  if (dtype == MFG_F64)
+    MFG_LAUNCH(MFG_PROF_SUB, es * (k + 1.0) * n * p, 2.0 * k * n * p,
+               launch_basis_combine<double>((const double *)Q, k, ld, n, p, coef, (double *)out, s));
+  else
+    MFG_LAUNCH(MFG_PROF_SUB, es * (k + 1.0) * n * p, 2.0 * k * n * p,
+               launch_basis_combine<float>((const float *)Q, k, ld, n, p, coef, (float *)out, s));
+  return MFG_OK;
 }
 
 int mfg_tridiag_eigh(int64_t k, int64_t p, const double *H, double *eigvals, double *eigvecs,

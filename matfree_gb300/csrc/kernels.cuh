@@ -88,8 +88,12 @@ int launch_adj_step_coef(const double *H, const double *Pi, const double *g, con
                          int k, int64_t p, int idx, double *Gamma, double *coefG, double *bp,
                          double *scal, double *beta, cudaStream_t s);
 template <typename T>
-int launch_adj_lincomb(const T *U, const T *lam, const T *R, const double *scal, int64_t n,
-                       int64_t ld, int64_t p, T *out, cudaStream_t s);
+int launch_adj_lincomb(const T *U, const T *lam, const T *R, const T *dq, int64_t dq_bstride,
+                       const double *scal, int64_t n, int64_t ld, int64_t p, T *out, cudaStream_t s);
+int launch_axpy_f64(double a, const double *x, double *y, int64_t m, cudaStream_t s);
+template <typename T>
+int launch_basis_combine(const T *Q, int64_t k, int64_t ld, int64_t n, int64_t p, const double *coef,
+                         T *out, cudaStream_t s);
 
 // tridiag_quadrature.cu
 int launch_tridiag_eigh_full(int64_t k, int64_t p, const double *H, double *w, double *S,

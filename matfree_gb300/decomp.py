@@ -136,12 +136,31 @@ class _Decomposition:
                              init_length_inv=c[0])
 
 
+def _differentiable_forward(dec, op, k, V):
+    """run_hessenberg with full reorthogonalisation, behind the Hessenberg
+    adjoint when V or the matvec's parameters require gradients (the custom
+    VJP of matfree/decomp.py:393-422); plain otherwise."""
+    from .autodiff import arnoldi_full, wants_grad
+
+    if k > 0 and wants_grad(V, op):
+        if not dec.custom_vjp:
+            raise NotImplementedError(
+                "gradients of the decomposition need custom_vjp=True: the Krylov loop runs as CUDA "
+                "kernels, so it is differentiated by the Hessenberg adjoint, not traced")
+        return arnoldi_full(op, k, V)
+    return run_hessenberg(op, k, V, reortho=full_reortho(op, k))
+
+
 class _TridiagSymFull(_Decomposition):
     def batched(self, matvec, V: torch.Tensor, *params) -> _DecompResult:
-        """Decompose every row of V (p, n) at once; outputs carry a leading p axis."""
+        """Decompose every row of V (p, n) at once; outputs carry a leading p axis.
+
+        Differentiable in V and in the tensor leaves of a callable matvec's
+        parameters (custom_vjp=True, the default)."""
+        V = require_cuda(V, "vectors")
         op = as_operator(matvec, V.shape[1], V.dtype, params)
         k = self.num_matvecs
-        Q, H, r, c = run_hessenberg(op, k, V, reortho=full_reortho(op, k))
+        Q, H, r, c = _differentiable_forward(self, op, k, V)
         d, e = _tridiag_from_hessenberg(H)
         out_dt = V.dtype if V.dtype in (torch.float32, torch.float64) else torch.float32
         d, e = d.to(out_dt), e.to(out_dt)
@@ -174,10 +193,17 @@ class _Hessenberg(_Decomposition):
         self.reortho_vjp = reortho if reortho_vjp == "match" else reortho_vjp
 
     def batched(self, matvec, V: torch.Tensor, *params) -> _DecompResult:
+        V = require_cuda(V, "vectors")
         op = as_operator(matvec, V.shape[1], V.dtype, params)
         k = self.num_matvecs
-        mode = full_reortho(op, k) if self.reortho == "full" else self.reortho
-        Q, H, r, c = run_hessenberg(op, k, V, reortho=mode)
+        if self.reortho == "full":
+            Q, H, r, c = _differentiable_forward(self, op, k, V)
+        else:
+            from .autodiff import wants_grad
+
+            if k > 0 and wants_grad(V, op):
+                raise NotImplementedError("gradients are provided for reortho='full' only")
+            Q, H, r, c = run_hessenberg(op, k, V, reortho=self.reortho)
         out_dt = V.dtype if V.dtype in (torch.float32, torch.float64) else torch.float32
         return _DecompResult(Q_tall=Q, J_small=H.to(out_dt), residual=r, init_length_inv=c.to(out_dt))
 

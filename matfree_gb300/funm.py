@@ -217,25 +217,47 @@ def monte_carlo_funm_sym_logdet(tridiag_sym, /):
 integrand_funm_sym_logdet = monte_carlo_funm_sym_logdet
 
 
-def funm_lanczos_sym(dense_funm, tridiag_sym, /):
-    """f(A) v via Lanczos (matfree/funm.py:114-147): ||v|| Q^T f(T) e1."""
-    if not isinstance(dense_funm, DenseFunmSymEigh):
-        dense_funm = DenseFunmSymEigh(dense_funm)
+class FunmLanczosSym:
+    """f(A) v by Lanczos: ||v|| Q^T f(T) e1 (matfree/funm.py:114-147).
 
-    def estimate(matvec, vec, *parameters):
+    ``batched(matvec, V)`` evaluates every row of V (p, n) at once: one batched
+    decomposition, the device eigensolver for f(T) e1 (mfg_tridiag_eigh, every
+    eigenvector) and the device back-projection Q^T (f(T) e1)
+    (mfg_basis_combine).  With the decomposition's custom VJP the result is
+    differentiable in V and in a callable matvec's parameters.
+    """
+
+    def __init__(self, dense_funm, tridiag_sym):
+        if not isinstance(dense_funm, DenseFunmSymEigh):
+            dense_funm = DenseFunmSymEigh(dense_funm)
+        self.dense_funm = dense_funm
+        self.tridiag_sym = tridiag_sym
+
+    def __call__(self, matvec, vec, *parameters):
         flat, unravel = ravel_pytree(vec)
         flat = require_cuda(flat, "vec")
-        length = torch.linalg.vector_norm(flat)
-        Q, T, *_ = tridiag_sym(_flat_operator(matvec, unravel, flat.numel(), flat.dtype, parameters)
-                               if not isinstance(matvec, Operator) else matvec, flat / length)
+        op = _flat_operator(matvec, unravel, flat.numel(), flat.dtype, parameters) \
+            if not isinstance(matvec, Operator) else matvec
+        return unravel(self.batched(op, flat[None, :])[0])
+
+    def batched(self, matvec, V: torch.Tensor, *parameters) -> torch.Tensor:
+        from .autodiff import basis_combine, funm_e1
+        from .decomp import _todense_tridiag_sym
+
+        V = require_cuda(V, "vectors")
+        length = torch.linalg.vector_norm(V, dim=1)
+        Q, T, *_ = self.tridiag_sym.batched(matvec, V / length[:, None], *parameters)
         if isinstance(T, tuple):
-            from .decomp import _todense_tridiag_sym
-
             T = _todense_tridiag_sym(*T)
-        fT = dense_funm(T.double())
-        return unravel(length * (Q.double().T @ fT[:, 0]).to(flat.dtype))
+        if T.shape[-1] == 0:
+            return torch.zeros_like(V)
+        coef = funm_e1(T, self.dense_funm) * length.to(torch.float64)[:, None]
+        return basis_combine(Q, coef).to(V.dtype)
 
-    return estimate
+
+def funm_lanczos_sym(dense_funm, tridiag_sym, /):
+    """f(A) v via Lanczos (matfree/funm.py:114-147): ||v|| Q^T f(T) e1."""
+    return FunmLanczosSym(dense_funm, tridiag_sym)
 
 
 # ---------------------------------------------------------------------------

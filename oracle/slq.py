@@ -151,6 +151,20 @@ def monte_carlo_funm_sym_logdet(num_matvecs):
     return monte_carlo_funm_sym(dense_funm_sym_eigh(np.log), num_matvecs)
 
 
+def funm_lanczos_sym(dense_funm, num_matvecs):
+    """matfree/funm.py:114-147: f(A) v = ||v|| Q^T f(T) e1 (Q_tall (k, n))."""
+
+    def estimate(matvec, vec):
+        vec = np.asarray(vec, dtype=np.float64)
+        length = np.linalg.norm(vec)
+        Q, dense, *_ = tridiag_sym_full(matvec, num_matvecs, vec / length, materialize=True)
+        fA = dense_funm(dense)
+        e1 = np.eye(len(dense))[0, :]
+        return length * (Q.T @ (fA @ e1))
+
+    return estimate
+
+
 def estimator_monte_carlo(integrand, matvec, samples):
     """matfree/stochtrace.py:47-50: mean of the integrand over the samples."""
     vals = np.array([integrand(matvec, s) for s in samples])

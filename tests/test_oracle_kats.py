@@ -256,3 +256,16 @@ def test_slq_gradient_rbf_matches_central_differences():
         e[i] = h
         fd = (value(theta + e) - value(theta - e)) / (2 * h)
         assert np.isclose(grad[i], fd, rtol=1e-5, atol=1e-6), (i, grad[i], fd)
+
+
+# tests/test_funm/test_funm_lanczos_sym.py:7-37 (sin, n = 11, k = 6, atol 1e-6)
+def test_funm_lanczos_sym_matches_eigh_implementation():
+    n = 11
+    rng = np.random.default_rng(2)
+    v = rng.standard_normal(n)
+    A = problems.hermitian_matrix_from_eigenvalues(np.linspace(0.01, 0.99, num=n), np.random.default_rng(1))
+    w, U = np.linalg.eigh(A)
+    expected = U @ np.diag(np.sin(w)) @ U.T @ v
+    fn = slq.funm_lanczos_sym(slq.dense_funm_sym_eigh(np.sin), 6)
+    received = fn(lambda x: A @ x, v)
+    assert np.allclose(expected, received, atol=1e-6)

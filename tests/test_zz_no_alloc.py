@@ -90,8 +90,12 @@ def test_noalloc_dense_apply_matches_float64_product_twice(precision, n, p):
 
 def test_noalloc_csr_apply_matches_float64_product_twice():
     m = 200
-    L = sp.random(m * m, m * m, density=5.0 / (m * m), format="csr", random_state=3, dtype=np.float32)
-    L = (L + sp.eye(m * m, dtype=np.float32)).tocsr()
+    n = m * m
+    rng0 = np.random.default_rng(3)
+    rows = np.repeat(np.arange(n), 5)
+    cols = rng0.integers(0, n, size=5 * n)
+    L = sp.csr_matrix((rng0.standard_normal(5 * n).astype(np.float32), (rows, cols)), shape=(n, n))
+    L = (L + sp.eye(n, dtype=np.float32)).tocsr()
     op = mf.CSROperator.from_scipy(L, shift=0.5)
     L64 = L.astype(np.float64)
     rng = np.random.default_rng(5)
@@ -127,10 +131,13 @@ def test_noalloc_limit_is_exactly_the_documented_condition():
     torch.cuda.synchronize()
     # A = I and V = 1: the product of the accepted call is V itself
     assert torch.equal(W[:p_max], V[:p_max])
-    # bf16 keeps one copy: twice the probes fit
+    # bf16 keeps one copy: 256 + round_up(p * ld * 2, 256) <= 32 MiB
     op1 = mf.DenseOperator(A, precision="bf16")
-    V1 = torch.ones((2 * p_max + 1, ld), dtype=torch.float32, device="cuda")
-    assert _status_noalloc(op1, 2 * p_max + 1, ld, V1, torch.zeros_like(V1)) == _lib.MFG_ERR_SCRATCH_LIMIT
+    p1 = (LIMIT - 256) // (ld * 2)
+    V1 = torch.ones((p1 + 1, ld), dtype=torch.float32, device="cuda")
+    W1 = torch.zeros_like(V1)
+    assert _status_noalloc(op1, p1 + 1, ld, V1, W1) == _lib.MFG_ERR_SCRATCH_LIMIT
+    assert _status_noalloc(op1, p1, ld, V1, W1) == _lib.MFG_OK
     # fp32 needs no copy and is never rejected for size
     op32 = mf.DenseOperator(A, precision="fp32")
     assert _status_noalloc(op32, p_max + 1, ld, V, W) == _lib.MFG_OK
