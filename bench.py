@@ -44,6 +44,9 @@ CONFIGS = {
     # for captures of the full-size operator apply
     "rbf16k4": ("rbf", 16384, 4, 256),
     "dense1k": ("dense", 1000, 30, 100),
+    # the sparse config's operator and panel at depth 4 (basis 1.07 GB), for
+    # captures of the sparse product
+    "laplace1m4": ("csr", 1024 * 1024, 4, 64),
     "laplace1m": ("csr", 1024 * 1024, 100, 64),
 }
 METRIC = "logdet solves/s"
@@ -158,7 +161,7 @@ def build_problem(cfg, seed=0):
         return {"kind": kind, "n": n, "k": k, "p": p, "x": x, "s2": 1.0, "ell": 0.2, "tau": 1e-2}
     if kind == "dense":
         B = np.random.default_rng(seed).standard_normal((n, n))
-        return {"kind": kind, "n": n, "k": k, "p": p, "A": (B @ B.T / n + np.eye(n)).astype(np.float32)}
+        return {"kind": kind, "n": n, "k": k, "p": p, "A": B @ B.T / n + np.eye(n)}
     m = int(round(math.sqrt(n)))
     import scipy.sparse as sp
 
@@ -410,7 +413,7 @@ def roofline(prof, peaks, steps, config=None, precision=None):
     launches = max(prof["apply"]["launches"], 1)
     if fl > 0:
         achieved = (fl / launches) / (apply_ms / 1e3 / launches) / 1e12
-        peak = peaks["tensor_sustained"]
+        peak = peaks["tensor_burst"]
         return {"kernel": "operator apply", "bound": "tensor", "achieved": achieved, "peak": peak,
                 "unit": "TFLOP/s", "frac": achieved / peak,
                 "traffic": TRAFFIC.get((config, precision, "operator apply")),
@@ -530,9 +533,50 @@ def _config(args):
     kind, n, k, p = CONFIGS[args.config]
     desc = {"rbf": "dense RBF kernel log-det (x~U[0,1]^3, ell=0.2, tau=1e-2)",
             "dense": "dense SPD B B^T/n + I log-det", "csr": "5-point Laplacian + 0.1 I log-det (CSR)"}[kind]
-    return {"workload": f"{desc}, n={n}, k={k}, p={p} Rademacher probes, operator {args.precision}",
+    opdesc = "CSR fp32 (int32 indices)" if kind == "csr" else args.precision
+    return {"workload": f"{desc}, n={n}, k={k}, p={p} Rademacher probes, operator {opdesc}",
             "n": n, "k": k, "p": p, "precision": args.precision, "parallelism": "replicas",
             "l2": "inputs larger than L2 (operator and Krylov basis > 129 MB); no flush"}
+
+
+def _profiled(fn, steps):
+    """Run fn() `steps` times with every library launch bracketed by CUDA
+    events; returns the per-class profile (ms, bytes, flops, launches)."""
+    import ctypes
+
+    import torch
+
+    from matfree_gb300 import _lib
+
+    lib = _lib.lib()
+    nc = len(_lib.PROF_CLASSES)
+    lib.mfg_profile_enable(1)
+    torch.cuda.synchronize()
+    for _ in range(steps):
+        fn()
+    torch.cuda.synchronize()
+    ms, by, fl = (ctypes.c_double * nc)(), (ctypes.c_double * nc)(), (ctypes.c_double * nc)()
+    ln = (ctypes.c_int64 * nc)()
+    _lib.check(lib.mfg_profile_read(nc, ms, by, fl, ln), "mfg_profile_read")
+    lib.mfg_profile_enable(0)
+    return {c: {"ms": ms[i], "bytes": by[i], "flops": fl[i], "launches": int(ln[i])}
+            for i, c in enumerate(_lib.PROF_CLASSES)}
+
+
+def _launch_count(fn, steps):
+    """Library kernel launches of `steps` calls of fn()."""
+    import ctypes
+
+    from matfree_gb300 import _lib
+
+    lib = _lib.lib()
+    nc = len(_lib.PROF_CLASSES)
+    lib.mfg_profile_enable(0)
+    for _ in range(steps):
+        fn()
+    ln = (ctypes.c_int64 * nc)()
+    _lib.check(lib.mfg_profile_read(nc, None, None, None, ln), "mfg_profile_read")
+    return int(sum(ln))
 
 
 def grad_arm(args):
@@ -559,24 +603,27 @@ def grad_arm(args):
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        val, grad = step()
-    torch.cuda.synchronize()
-    secs = (time.perf_counter() - t0) / args.steps
-    # float64 oracle gradient on the first probes (same probe vectors)
+    with ClockSampler(0) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            val, grad = step()
+        torch.cuda.synchronize()
+        secs = (time.perf_counter() - t0) / args.steps
+    clocks = clk.summary()
+    launches = _launch_count(step, 1) * args.steps
+    prof = _profiled(step, args.steps)
+    rl = roofline(prof, _peaks(), args.steps)
+    rl["peak_source"] = f"of {_peaks()['source']}"
+    # float64 oracle gradient on every probe (same probe vectors)
     from oracle import adjoint as oadj
     from oracle import philox
 
-    num = args.cpu_probes
-    Vs = philox.rademacher(np.asarray(key, np.uint32), num, n)
+    Vs = philox.rademacher(np.asarray(key, np.uint32), p, n)
     t1 = time.perf_counter()
     matmat, vjp_matmat = oadj.rbf_vjp_factory(x.astype(np.float64), theta0)
-    _, g_ref = oadj.slq_grad_batched(matmat, vjp_matmat, 3, k, Vs)
+    v_ref, g_ref = oadj.slq_grad_batched(matmat, vjp_matmat, 3, k, Vs)
     cpu_s = time.perf_counter() - t1
-    th = torch.tensor(theta0, dtype=torch.float64, requires_grad=True)
-    autodiff.rbf_logdet(xd, th, V[:num], k, precision=args.precision).backward()
-    g_gpu = th.grad.numpy()
+    g_gpu = grad.numpy()
     rel = np.abs(g_gpu - g_ref) / np.abs(g_ref)
     line = {"metric": "logdet+grad solves/s", "value": 1.0 / secs, "unit": "solves/s", "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs, "higher_is_better": True,
@@ -584,11 +631,14 @@ def grad_arm(args):
             "data": "synthetic (seeded)",
             "config": {"workload": f"GP log-det + d/dtheta, RBF n={n}, k={k}, p={p}, theta=(0, log 0.2, log 1e-2)"},
             "estimate": float(val), "grad": grad.tolist(),
-            "grad_rel_err_vs_fp64_oracle": {"value": rel.tolist(), "on": f"first {num} probes, identical probes"},
-            "cpu_baseline": {"value": 1.0 / (cpu_s * p / num), "unit": "solves/s",
+            "rel_err_vs_fp64": {"value": abs(float(val) - v_ref) / abs(v_ref), "on": f"all {p} probes"},
+            "grad_rel_err_vs_fp64_oracle": {"value": rel.tolist(), "on": f"all {p} probes, identical probes"},
+            "roofline": rl, "clocks": clocks, "gpu_launches": launches,
+            "kernel_ms_per_step": {c: v["ms"] / args.steps for c, v in prof.items()},
+            "cpu_baseline": {"value": 1.0 / cpu_s, "unit": "solves/s",
                              "cores": len(os.sched_getaffinity(0)), "kind": "port",
-                             "sample": f"{num} of {p} probes (float64 forward + adjoint restatement), "
-                                       "extrapolated linearly in probes"}}
+                             "sample": f"one complete solve: value and gradient on all {p} probes "
+                                       "(float64 forward + adjoint restatement)"}}
     print(json.dumps(line), flush=True)
 
 
@@ -709,26 +759,74 @@ def product_arm(args):
     print(json.dumps(line), flush=True)
 
 
+def _plain_fp32_request(req, dev="cuda"):
+    """One request the plain way: fp32 RBF operator, the operator product as a
+    cuBLAS SGEMM (TF32 off) called back once per Krylov step, one request at a
+    time (the per-request FP32 drop-in of the serving comparison)."""
+    import torch
+
+    import matfree_gb300 as mf
+    from matfree_gb300 import serve
+    from matfree_gb300.funm import slq_values
+
+    n = req.x.shape[0]
+    xd = torch.from_numpy(np.ascontiguousarray(req.x, dtype=np.float32)).to(dev)
+    op = mf.RBFKernelOperator(xd, s2=req.s2, ell=req.ell, tau=req.tau, precision="fp32")
+    K = op.a[:, :n]
+    cb = mf.CallbackOperator(lambda X: torch.addmm(X, X, K, beta=req.tau), n, batched=True)
+    V = mf.stochtrace.sampler_signs(torch.ones(n, device=dev), num=req.p)(np.asarray(req.key, np.uint32))
+    fun, param = serve._fun_code(req.fun)
+    return slq_values(cb, req.k, V, fun, param).mean()
+
+
 def serve_arm(args):
-    """Mixed request stream through the continuous-batching server vs one-by-one fp32."""
+    """The serving stream through the continuous-batching server, with the plain
+    per-request FP32 path timed on a prefix of the same stream and the served
+    values checked against the float64 oracle on a seeded subset of requests."""
     import torch
 
     from matfree_gb300 import serve
+    from oracle import philox, problems, slq
 
     torch.cuda.set_device(0)
     reqs = serve.synthetic_stream(args.requests, rate=args.rate, seed=0)
-    warm = serve.synthetic_stream(4, rate=1e6, seed=99)
+    warm = serve.synthetic_stream(8, rate=1e6, seed=99)
     srv = serve.SLQServer(slots=args.slots, budget_bytes=150e9, precision="bf16x3")
     srv.run(warm, realtime=False)
     torch.cuda.synchronize()
     with ClockSampler(0) as clk:
         res, stats = srv.run(reqs, realtime=True)
     clocks = clk.summary()
-    plain = serve.SLQServer(slots=1, budget_bytes=150e9, precision="fp32")
-    plain.run(warm[:1], realtime=False)
+    by_id = {r.rid: r for r in res}
+    # plain per-request FP32 (cuBLAS SGEMM, TF32 off) on a prefix of the stream
+    tf32 = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
     base_reqs = reqs[: args.baseline_requests] if args.baseline_requests > 0 else reqs
-    _, bstats = plain.run(base_reqs, realtime=False)
-    work = sum(2.0 * r.x.shape[0] ** 2 * r.p * r.k * 3 for r in reqs)
+    _plain_fp32_request(warm[0])
+    torch.cuda.synchronize()
+    t_p = time.perf_counter()
+    for r in base_reqs:
+        float(_plain_fp32_request(r))
+    plain_s = time.perf_counter() - t_p
+    torch.backends.cuda.matmul.allow_tf32 = tf32
+    # the served value against the float64 oracle: the three largest requests
+    # whose float64 solve stays under 6e12 flop, and the smallest request
+    cost = {r.rid: 2.0 * r.x.shape[0] ** 2 * r.p * r.k for r in reqs}
+    big = sorted((r for r in reqs if cost[r.rid] <= 6e12), key=lambda r: -r.x.shape[0])[:3]
+    chosen = big + [min(reqs, key=lambda r: r.x.shape[0])]
+    errs = []
+    for r in chosen:
+        K = problems.rbf_kernel(r.x.astype(np.float64), r.s2, r.ell, r.tau)
+        V = philox.rademacher(np.asarray(r.key, np.uint32), r.p, r.x.shape[0])
+        f = np.log if r.fun == "log" else (lambda t, a=float(r.fun.split(":")[1]): np.exp(a * t))
+        want = slq.slq_batched(lambda X: X @ K, r.k, V, matfun=f).mean()
+        del K
+        errs.append({"rid": r.rid, "n": r.x.shape[0], "k": r.k, "p": r.p, "fun": r.fun,
+                     "rel_err": abs(by_id[r.rid].mean - want) / abs(want)})
+    work = sum(6.0 * r.x.shape[0] ** 2 * r.p * r.k for r in reqs)  # bf16x3: three products per step
+    peaks = _peaks()
+    tflops = work / stats["wall_s"] / 1e12
+    plain_rate = len(base_reqs) / plain_s
     line = {"metric": METRIC, "value": stats["solves_per_s"], "unit": UNIT, "n_gpus": 1,
             "steps": len(reqs), "warmup": len(warm), "ms_per_step": 1e3 * stats["wall_s"] / len(reqs),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -738,11 +836,49 @@ def serve_arm(args):
                                    "{16,32,64,96}, p in {32,64,128,256}, bf16x3 operators built per request",
                        "slots": args.slots, "budget_gb": 150, "parallelism": "streams"},
             "latency_ms": {"p50": stats["p50_ms"], "p99": stats["p99_ms"], "mean": stats["mean_ms"]},
-            "plain_fp32_per_request": {"solves_per_s": bstats["solves_per_s"], "requests": len(base_reqs),
-                                       "note": "same requests one at a time, fp32 CUDA-core operator"},
-            "speedup_vs_plain_fp32": stats["solves_per_s"] / bstats["solves_per_s"],
-            "operator_tflop_per_s": work / stats["wall_s"] / 1e12, "clocks": clocks}
+            "rel_err_vs_fp64": {"value": max(e["rel_err"] for e in errs), "on": errs},
+            "plain_fp32_per_request": {"solves_per_s": plain_rate, "requests": len(base_reqs),
+                                       "note": "the first requests of the same stream one at a time: fp32 "
+                                               "operator, cuBLAS SGEMM (TF32 off) per Krylov step"},
+            "speedup_vs_plain_fp32": stats["solves_per_s"] / plain_rate,
+            "roofline": {"kernel": "operator products of all requests (bf16x3 tensor-core GEMMs)",
+                         "bound": "tensor", "achieved": tflops, "peak": peaks["tensor_burst"],
+                         "unit": "TFLOP/s", "frac": tflops / peaks["tensor_burst"], "traffic": None,
+                         "peak_source": f"of {peaks['source']}",
+                         "note": "algorithmic operator flops of the whole stream over its wall time"},
+            "clocks": clocks}
     print(json.dumps(line), flush=True)
+
+
+# The other benchmark configurations, run after the headline measurement of a
+# default invocation (each in its own process, so that a failure in one cannot
+# take the headline line with it) and reported under "other_configs".
+OTHER_CONFIGS = [
+    ("dense1k_fp64", ["--config", "dense1k", "--precision", "fp64", "--steps", "20"]),
+    ("laplace1m", ["--config", "laplace1m", "--steps", "3"]),
+    ("grad8k", ["--config", "grad8k", "--steps", "5"]),
+    ("product8k", ["--config", "product8k", "--steps", "5"]),
+    ("gp8k", ["--config", "gp8k", "--steps", "2"]),
+    ("serve", ["--config", "serve"]),
+]
+
+
+def run_other_configs(timeout_s=900):
+    out = {}
+    for name, argv in OTHER_CONFIGS:
+        cmd = [sys.executable, os.path.abspath(__file__), *argv, "--warmup", "3", "--no-other-configs"]
+        t0 = time.perf_counter()
+        try:
+            proc = subprocess.run(cmd, capture_output=True, text=True, timeout=timeout_s)
+            lines = [ln for ln in proc.stdout.splitlines() if ln.startswith("{")]
+            if proc.returncode == 0 and lines:
+                out[name] = json.loads(lines[-1])
+            else:
+                out[name] = {"error": f"rc {proc.returncode}", "stderr_tail": proc.stderr[-2000:]}
+        except subprocess.TimeoutExpired:
+            out[name] = {"error": f"timed out after {timeout_s} s"}
+        out[name]["run_s"] = time.perf_counter() - t0
+    return out
 
 
 def main():
@@ -752,16 +888,18 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="rbf16k", choices=sorted(CONFIGS) + ["serve", "grad8k", "gp8k", "product8k"])
-    ap.add_argument("--requests", type=int, default=64)
-    ap.add_argument("--baseline-requests", type=int, default=0,
+    ap.add_argument("--requests", type=int, default=10000)
+    ap.add_argument("--baseline-requests", type=int, default=200,
                     help="requests of the plain fp32 comparison (0: all of them)")
-    ap.add_argument("--rate", type=float, default=150.0)
+    ap.add_argument("--rate", type=float, default=100.0)
     ap.add_argument("--slots", type=int, default=8)
     ap.add_argument("--inflight", type=int, default=3,
                     help="independent solves in flight (round-robin over CUDA streams)")
     ap.add_argument("--precision", default="bf16x3", choices=["fp32", "bf16", "bf16x3", "fp64"])
     ap.add_argument("--cpu-probes", type=int, default=8)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-other-configs", action="store_true",
+                    help="report the headline configuration only")
     ap.add_argument("--no-plain-fp32", action="store_true",
                     help="skip the plain per-request fp32 comparison solves")
     args = ap.parse_args()
@@ -810,6 +948,17 @@ def main():
                     else "three reads of the basis per step",
                     "retries": res["two_sweep_retries"]},
     }
+    if prob["kind"] == "csr":
+        # the sparse product (K2) beside the dominant class: algorithmic bytes
+        # 8 nnz + 4 (n + 1) + 8 n p per launch over its event-timed duration
+        ap = res["prof"]["apply"]
+        if ap["ms"] > 0:
+            gbs = ap["bytes"] / (ap["ms"] / 1e3) / 1e9
+            line["spmm_roofline"] = {"kernel": "csr_spmm_window_kernel", "bound": "hbm", "achieved": gbs,
+                                     "peak": peaks["hbm"], "unit": "GB/s", "frac": gbs / peaks["hbm"],
+                                     "launches": ap["launches"],
+                                     "ms_per_launch": ap["ms"] / max(ap["launches"], 1),
+                                     "peak_source": f"of {peaks['source']}"}
     if not args.no_cpu_baseline:
         # one complete float64 solve on the host cores: every probe, full n and k
         # (a probe subset only where the bases would not fit in host memory)
@@ -843,6 +992,12 @@ def main():
             for name in ("simt", "cublas"):
                 line["plain_fp32_per_request"][f"{name}_rel_err_vs_fp64"] = rel_err_summary(
                     pl[name]["values"].cpu().numpy(), vals)["value"]
+    if args.config == "rbf16k" and world == 1 and not args.no_other_configs:
+        del res
+        import torch
+
+        torch.cuda.empty_cache()
+        line["other_configs"] = run_other_configs()
     print(json.dumps(line), flush=True)
 
 

@@ -103,31 +103,69 @@ def _dlog(x):
     return 1.0 / x
 
 
+def backward_bytes_per_probe(n: int, k: int, dtype=torch.float32) -> int:
+    """Device bytes one probe holds between the forward and the backward pass
+    (Krylov basis Q, adjoint states Lambda and the residual, in the basis type)."""
+    es = 8 if dtype == torch.float64 else 4
+    return int((2 * k + 1) * padded_ld(n) * es)
+
+
+def probe_chunks(p: int, n: int, k: int, dtype, budget_bytes) -> list:
+    """Probe ranges [b0, b1) whose bases fit ``budget_bytes`` (all probes at once
+    when no budget is given or they fit)."""
+    if budget_bytes is None:
+        return [(0, p)]
+    per = backward_bytes_per_probe(n, k, dtype)
+    pc = max(1, min(p, int(budget_bytes // per)))
+    return [(b0, min(p, b0 + pc)) for b0 in range(0, p, pc)]
+
+
 class _RBFLogdet(torch.autograd.Function):
-    """mean_b ||v_b||^2 e1^T log(T_b) e1 for K(theta), differentiable in theta."""
+    """mean_b ||v_b||^2 e1^T log(T_b) e1 for K(theta), differentiable in theta.
+
+    When the bases of all probes (Q, Lambda, residual: (2k + 1) n elements per
+    probe) exceed ``budget_bytes``, the probes are processed in chunks that
+    fit: the forward pass keeps only each chunk's H and 1/||v||, and the
+    backward pass recomputes the chunk's Krylov basis (the same deterministic
+    kernels on the same probes) before running its adjoint.  Probes are
+    independent, so the gradient is that of the unchunked computation."""
 
     @staticmethod
-    def forward(ctx, theta, x, probes, k, precision):
+    def forward(ctx, theta, x, probes, k, precision, budget_bytes):
         s2, ell, tau = (float(math.exp(t)) for t in theta.detach().cpu().tolist())
         op = RBFKernelOperator(x, s2=s2, ell=ell, tau=tau, precision=precision)
         n = op.n
         panel, ld = as_panel(probes, n, op.basis_dtype)
         p = panel.shape[0]
-        Q, H, R, c = _forward_panels(op, k, panel, ld)
-        scale = 1.0 / (c * c)
-        values, dH = quadform_dH(H, scale, _log, _dlog)
+        chunks = probe_chunks(p, n, k, op.basis_dtype, budget_bytes)
+        vals, saved = [], []
+        for b0, b1 in chunks:
+            Q, H, R, c = _forward_panels(op, k, panel[b0:b1], ld)
+            values, dH = quadform_dH(H, 1.0 / (c * c), _log, _dlog)
+            vals.append(values)
+            if len(chunks) == 1:
+                saved.append((Q, H, R, c, dH))
+            else:
+                del Q, R  # recomputed in the backward pass
+                saved.append((None, H, None, c, dH))
         ctx.save_for_backward(theta, x)
-        ctx.saved = (op, Q, H, R, c, dH, p, precision)
-        return values.mean()
+        ctx.saved = (op, panel, ld, chunks, saved, p, precision)
+        return torch.cat(vals).mean()
 
     @staticmethod
     def backward(ctx, grad_out):
         theta, x = ctx.saved_tensors
-        op, Q, H, R, c, dH, p, precision = ctx.saved
-        dH = dH * (grad_out.double() / p)
-        Lam, _dv = hessenberg_adjoint(op, Q, H, R, c, dH)
-        grad = rbf_theta_contractions(op, x, Q, Lam)
-        return grad.to(device=theta.device, dtype=theta.dtype), None, None, None, None
+        op, panel, ld, chunks, saved, p, precision = ctx.saved
+        grad = None
+        dl = _rbf_dlogell_operator(op, x)
+        for (b0, b1), (Q, H, R, c, dH) in zip(chunks, saved):
+            if Q is None:
+                Q, H, R, c = _forward_panels(op, H.shape[-1], panel[b0:b1], ld)
+            Lam, _dv = hessenberg_adjoint(op, Q, H, R, c, dH * (grad_out.double() / p))
+            g = rbf_theta_contractions(op, x, Q, Lam, dl=dl)
+            grad = g if grad is None else grad + g
+            del Q, R, Lam
+        return grad.to(device=theta.device, dtype=theta.dtype), None, None, None, None, None
 
 
 def _forward_panels(op, k, panel, ld):
@@ -164,7 +202,7 @@ def _forward_panels(op, k, panel, ld):
     return Q, H, R, c
 
 
-def rbf_theta_contractions(op: RBFKernelOperator, x, Q, Lam) -> torch.Tensor:
+def rbf_theta_contractions(op: RBFKernelOperator, x, Q, Lam, dl=None) -> torch.Tensor:
     """d/dtheta of sum_idx lambda_idx^T K(theta) q_idx for theta = (log s2, log ell, log tau).
 
     dK/dlog s2 = K - tau I,  dK/dlog ell = s2 E o D / ell^2,  dK/dlog tau = tau I.
@@ -176,7 +214,8 @@ def rbf_theta_contractions(op: RBFKernelOperator, x, Q, Lam) -> torch.Tensor:
     # the stored exponential part (without the nugget) is dK/dlog s2
     base = DenseOperator._from_storage(n, op.precision, op.a, op.a_lo, 0.0)
     g0 = (lam * base.matmat(rows).double()).sum()
-    dl = _rbf_dlogell_operator(op, x)
+    if dl is None:
+        dl = _rbf_dlogell_operator(op, x)
     g1 = (lam * dl.matmat(rows).double()).sum()
     g2 = op.tau * (lam * rows.double()).sum()
     return torch.stack([g0, g1, g2])
@@ -196,11 +235,14 @@ def _rbf_dlogell_operator(op: RBFKernelOperator, x) -> DenseOperator:
 
 
 def rbf_logdet(x: torch.Tensor, theta: torch.Tensor, probes: torch.Tensor, num_matvecs: int,
-               precision: str = "bf16x3") -> torch.Tensor:
+               precision: str = "bf16x3", budget_bytes=None) -> torch.Tensor:
     """SLQ estimate of log det K(theta) on the given probes, differentiable in theta.
 
     theta = (log s2, log ell, log tau) as a CUDA or CPU tensor of 3 values;
-    probes (p, n) CUDA tensor; returns a 0-d float64 tensor.
+    probes (p, n) CUDA tensor; returns a 0-d float64 tensor.  ``budget_bytes``
+    caps the device memory the Krylov bases hold between the forward and the
+    backward pass (probe chunks recomputed in the backward pass; see
+    ``backward_bytes_per_probe``).
     """
     x = require_cuda(x, "x")
     probes = require_cuda(probes, "probes")
@@ -208,7 +250,8 @@ def rbf_logdet(x: torch.Tensor, theta: torch.Tensor, probes: torch.Tensor, num_m
         from .decomp import _error_num_matvecs
 
         raise ValueError(_error_num_matvecs(num_matvecs, maxval=x.shape[0], minval=0))
-    return _RBFLogdet.apply(theta, x.to(torch.float32).contiguous(), probes, int(num_matvecs), precision)
+    return _RBFLogdet.apply(theta, x.to(torch.float32).contiguous(), probes, int(num_matvecs), precision,
+                            budget_bytes)
 
 
 def _fun_pair(dense_funm):
@@ -488,4 +531,4 @@ def callback_quadform(fn, n: int, k: int, samples: torch.Tensor, dense_funm, par
 
 __all__ = ["quadform_dH", "hessenberg_adjoint", "rbf_logdet", "rbf_theta_contractions",
            "run_hessenberg", "callback_quadform", "params_require_grad", "arnoldi_full", "wants_grad",
-           "funm_e1", "basis_combine"]
+           "funm_e1", "basis_combine", "backward_bytes_per_probe", "probe_chunks"]

@@ -200,8 +200,8 @@ static int apply_op(const mfg_operator *op, const T *V, int64_t ldv, T *W, int64
       return MFG_ERR_UNSUPPORTED;
     case MFG_OP_CSR:
       if constexpr (sizeof(T) == 4)
-        return launch_csr_spmm(op->row_ptr, op->col_idx, op->values, n, V, ldv, W, ldw, p,
-                               op->shift, s);
+        return launch_csr_spmm(op->row_ptr, op->col_idx, op->values, n, op->nnz, V, ldv, W, ldw, p,
+                               op->shift, status, s);
       return MFG_ERR_UNSUPPORTED;
     case MFG_OP_CALLBACK: {
       const T *src = V;

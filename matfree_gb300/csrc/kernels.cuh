@@ -108,8 +108,8 @@ template <typename T>
 int launch_dense_simt(const T *A, int64_t lda, const T *V, int64_t ldv, T *W, int64_t ldw,
                       int64_t n, int64_t p, double shift, cudaStream_t s);
 int launch_csr_spmm(const int32_t *row_ptr, const int32_t *col_idx, const float *val, int64_t n,
-                    const float *V, int64_t ldv, float *W, int64_t ldw, int64_t p, double shift,
-                    cudaStream_t s);
+                    int64_t nnz, const float *V, int64_t ldv, float *W, int64_t ldw, int64_t p,
+                    double shift, int *status, cudaStream_t s);
 int launch_rbf_build(const float *x, int64_t n, int dim, double s2, double ell, int precision,
                      int dlogell, void *a, void *a_lo, int64_t lda, cudaStream_t s);
 int launch_split_bf16(const float *a, int64_t rows, int64_t cols, int64_t lda, __nv_bfloat16 *hi,

@@ -92,3 +92,20 @@ def asymmetric_matrix_from_singular_values(vals, nrows, ncols):
     A /= nrows * ncols
     U, _S, Vt = np.linalg.svd(A, full_matrices=False)
     return U @ np.diag(np.asarray(vals, dtype=np.float64)) @ Vt
+
+
+def random_csr(n, rng, lengths, band=None):
+    """CSR (float64) with lengths[r] entries in row r at distinct random columns,
+    within |c - r| <= band when a band is given (sparse-product test matrices)."""
+    rows, cols = [], []
+    for r in range(n):
+        k = int(min(lengths[r], n))
+        if band is None:
+            cc = rng.choice(n, size=k, replace=False)
+        else:
+            lo, hi = max(0, r - band), min(n, r + band + 1)
+            cc = rng.choice(np.arange(lo, hi), size=min(k, hi - lo), replace=False)
+        cols += list(cc)
+        rows += [r] * len(cc)
+    data = rng.standard_normal(len(rows))
+    return sp.csr_matrix((data, (rows, cols)), shape=(n, n))

@@ -161,6 +161,22 @@ def test_grad8k_gpu_gradient_matches_oracle(grad8k, precision, tol_val, tol_grad
     np.testing.assert_allclose(g, fd, rtol=tol_grad + 1e-6)
 
 
+def test_grad8k_gradient_under_a_memory_budget(grad8k):
+    # Krylov bases held between the passes capped at a quarter of Q + Lambda:
+    # probe chunks are recomputed in the backward pass; same gradient
+    x, theta0, V, k, val, grad, fd = grad8k
+    n, p = x.shape[0], V.shape[0]
+    budget = autodiff.backward_bytes_per_probe(n, k, torch.float64) * p / 4
+    assert len(autodiff.probe_chunks(p, n, k, torch.float64, budget)) >= 4
+    got = []
+    for b in (None, budget):
+        theta = torch.tensor(theta0, dtype=torch.float64, requires_grad=True)
+        autodiff.rbf_logdet(_t(x, torch.float32), theta, _t(V), k, precision="fp64", budget_bytes=b).backward()
+        got.append(theta.grad.numpy())
+    np.testing.assert_allclose(got[1], got[0], rtol=1e-10)
+    np.testing.assert_allclose(got[1], grad, rtol=1e-8)
+
+
 # -------------------------------------------------------------------- serve
 
 
