@@ -148,24 +148,25 @@ template int launch_dense_simt<double>(const double *, int64_t, const double *, 
 // The panels are probe-major, so the product is p sparse matrix-vector
 // products that share the CSR arrays.  The rows are cut into tiles of
 // kWRows; CTAs take tiles round-robin, so neighbouring tiles run at the same
-// time and the vector entries they share are served from L2.  Per tile:
-//   1. the row pointers and the tile's contiguous segment of column indices
-//      and values are staged in shared memory once, with 16-byte vector loads
-//      (aligned 4-entry chunks; a partial chunk at the end of the arrays, and
-//      arrays whose base is not 16-byte aligned, go entry by entry);
-//   2. the tile's column range [lo, hi] (including its own rows, for the
-//      shift term) gives the window of each probe vector that the tile reads.
-//      When it is at most kWMax entries (banded matrices: stencils of
+// time and the vector entries they share are served from L2.  (Equal tiles
+// sized to a whole number of waves measured slower on the 2-D Laplacian: the
+// smaller tiles re-read more of the neighbouring rows.)  Per tile:
+//   1. each row thread (4 rows per thread, rows r0 + t + 256 i) loads the
+//      first RMAX entries of its rows into registers once; the tile's column
+//      range [lo, hi] (including its own rows, for the shift term) follows
+//      from a block reduction;
+//   2. when the range is at most kWMax entries (banded matrices: stencils of
 //      bandwidth up to about (kWMax - kWRows) / 2), a copy warp streams probe
 //      b's window V[b][lo..hi] into a ring of shared-memory buffers with one
-//      1-D bulk copy (cp.async.bulk) per probe, and the eight row warps read
-//      every gather from shared memory: each probe vector is read from HBM
-//      about once, in long bursts, instead of as five scattered 4-byte
-//      gathers per product;
-//   3. otherwise (wide or random column patterns) the row warps gather from
+//      1-D bulk copy (cp.async.bulk) per probe, and the row threads form every
+//      product from registers and shared memory (one shared load and one FMA
+//      per entry): each probe vector is read from HBM about once, in long
+//      bursts, instead of as scattered 4-byte gathers;
+//   3. otherwise (wide or random column patterns) the row threads gather from
 //      global memory: lane = row for short rows, and a warp walks its rows
 //      one at a time with a butterfly of warp shuffles when one of them is
 //      longer than kWLong entries.
+// Entries beyond RMAX of a row are read from global memory in the same order.
 // Every sum runs in a fixed order, so results do not depend on timing.  All
 // waits are bounded (MFG_ERR_TIMEOUT in *status); after a failure the CTA
 // stops at the next tile boundary and drains its copies in flight.
@@ -175,9 +176,8 @@ constexpr int kWRows = 1024;                   // rows per tile
 constexpr int kWThreads = 256;                 // row threads (8 warps) + one copy warp
 constexpr int kWRowWarps = kWThreads / 32;
 constexpr int kWRowsPerThread = kWRows / kWThreads;
-constexpr int kWSeg = 6144;                    // staged CSR entries per tile
 constexpr int kWMax = 4096;                    // window entries per ring buffer (16 KB)
-constexpr int kWStages = 3;
+constexpr int kWStages = 6;
 constexpr int kWLong = 32;                     // longer rows take the warp-cooperative path
 
 struct WinShared {
@@ -185,8 +185,6 @@ struct WinShared {
   uint64_t empty[kWStages];
   int lo, hi, fail, pad;
   int32_t rp[kWRows + 4];
-  int32_t ci[kWSeg + 8];
-  float val[kWSeg + 8];
   float win[kWStages][kWMax];
 };
 
@@ -194,9 +192,10 @@ __device__ __forceinline__ uint32_t sp_smem(const void *p) {
   return (uint32_t)__cvta_generic_to_shared(p);
 }
 
-__global__ void __launch_bounds__(kWThreads + 32, 2)
+template <int RMAX>
+__global__ void __launch_bounds__(kWThreads + 32, RMAX <= 6 ? 2 : 1)
 csr_spmm_window_kernel(const int32_t *__restrict__ rp, const int32_t *__restrict__ ci,
-                       const float *__restrict__ val, int64_t n, int64_t nnz, int vec_ok,
+                       const float *__restrict__ val, int64_t n, int tile_rows,
                        const float *__restrict__ V, int64_t ldv, float *__restrict__ W, int64_t ldw,
                        int64_t p, float shift, int *status) {
   extern __shared__ __align__(128) uint8_t sp_raw[];
@@ -215,50 +214,44 @@ csr_spmm_window_kernel(const int32_t *__restrict__ rp, const int32_t *__restrict
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
-  const int64_t ntiles = (n + kWRows - 1) / kWRows;
+  const int64_t ntiles = (n + tile_rows - 1) / tile_rows;
   int64_t g = 0;          // window copies issued (copy warp) / consumed (row warps) by this CTA
   int64_t issued = 0;     // copy warp: for the drain after a failure
   for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     __syncthreads();  // the previous tile's shared data is no longer read
     if (*fail) break;  // uniform: read after the barrier
-    const int64_t r0 = tile * kWRows;
-    const int rows = (int)(n - r0 < (int64_t)kWRows ? n - r0 : (int64_t)kWRows);
+    const int64_t r0 = tile * tile_rows;
+    const int rows = (int)(n - r0 < (int64_t)tile_rows ? n - r0 : (int64_t)tile_rows);
     for (int i = threadIdx.x; i <= rows; i += kWThreads + 32) sh->rp[i] = __ldg(rp + r0 + i);
     if (threadIdx.x == 0) {
       sh->lo = (int)r0;
       sh->hi = (int)(r0 + rows - 1);
     }
     __syncthreads();
-    const int64_t e_begin = sh->rp[0], e_end = sh->rp[rows];
-    const int64_t a0 = e_begin & ~(int64_t)3;
-    const bool staged = e_end - a0 <= kWSeg;
-    if (staged) {
-      const int chunks = (int)((e_end - a0 + 3) >> 2);
+    // this thread's rows: the first RMAX entries in registers
+    int col[kWRowsPerThread][RMAX];
+    float a[kWRowsPerThread][RMAX];
+    int e0[kWRowsPerThread], len[kWRowsPerThread];
+    if (!copier) {
       int cmin = 0x7fffffff, cmax = -1;
-      for (int q = threadIdx.x; q < chunks; q += kWThreads + 32) {
-        const int64_t e = a0 + 4 * (int64_t)q;
-        int cc[4];
-        float vv[4];
-        if (vec_ok && e + 4 <= nnz) {
-          const int4 c4 = __ldg(reinterpret_cast<const int4 *>(ci + e));
-          const float4 v4 = __ldg(reinterpret_cast<const float4 *>(val + e));
-          cc[0] = c4.x; cc[1] = c4.y; cc[2] = c4.z; cc[3] = c4.w;
-          vv[0] = v4.x; vv[1] = v4.y; vv[2] = v4.z; vv[3] = v4.w;
-        } else {
 #pragma unroll
-          for (int t = 0; t < 4; ++t) {
-            cc[t] = e + t < nnz ? __ldg(ci + e + t) : 0;
-            vv[t] = e + t < nnz ? __ldg(val + e + t) : 0.f;
+      for (int i = 0; i < kWRowsPerThread; ++i) {
+        const int lr = threadIdx.x + i * kWThreads;
+        e0[i] = lr < rows ? sh->rp[lr] : 0;
+        len[i] = lr < rows ? sh->rp[lr + 1] - e0[i] : 0;
+#pragma unroll
+        for (int q = 0; q < RMAX; ++q) {
+          col[i][q] = q < len[i] ? __ldg(ci + e0[i] + q) : (int)(r0 + (lr < rows ? lr : 0));
+          a[i][q] = q < len[i] ? __ldg(val + e0[i] + q) : 0.f;
+          if (q < len[i]) {
+            cmin = min(cmin, col[i][q]);
+            cmax = max(cmax, col[i][q]);
           }
         }
-#pragma unroll
-        for (int t = 0; t < 4; ++t) {
-          sh->ci[4 * q + t] = cc[t];
-          sh->val[4 * q + t] = vv[t];
-          if (e + t >= e_begin && e + t < e_end) {
-            cmin = min(cmin, cc[t]);
-            cmax = max(cmax, cc[t]);
-          }
+        for (int e = e0[i] + RMAX; e < e0[i] + len[i]; ++e) {
+          const int c = __ldg(ci + e);
+          cmin = min(cmin, c);
+          cmax = max(cmax, c);
         }
       }
 #pragma unroll
@@ -276,14 +269,18 @@ csr_spmm_window_kernel(const int32_t *__restrict__ rp, const int32_t *__restrict
     const int64_t wlen = ((int64_t)sh->hi + 1 - lo + 3) & ~(int64_t)3;  // <= ld - lo: ld % 8 == 0
     // (column indices outside [0, n) break the caller's contract; such a tile
     // never issues a bulk copy)
-    const bool windowed = staged && wlen <= kWMax && sh->lo >= 0 && sh->hi < n;
+    const bool windowed = wlen <= kWMax && sh->lo >= 0 && sh->hi < n;
 
     if (windowed) {
       if (copier) {
         if (lane == 0) {
+          int s = (int)(g % kWStages);
+          uint32_t ph = (uint32_t)((g / kWStages) & 1);
           for (int64_t b = 0; b < p; ++b, ++g) {
-            const int s = (int)(g % kWStages);
-            const uint32_t ph = (uint32_t)((g / kWStages) & 1);
+            if (b > 0 && ++s == kWStages) {
+              s = 0;
+              ph ^= 1u;
+            }
             if (g >= kWStages && !mbar_wait_bounded(sp_smem(&sh->empty[s]), ph ^ 1u, fail)) {
               *fail = 1;
               if (status) atomicExch(status, (int)MFG_ERR_TIMEOUT);
@@ -304,10 +301,18 @@ csr_spmm_window_kernel(const int32_t *__restrict__ rp, const int32_t *__restrict
         g = __shfl_sync(0xffffffffu, g, 0);
         issued = __shfl_sync(0xffffffffu, issued, 0);
       } else {
-        const int t = threadIdx.x;
+        // byte offsets into the window: the columns, and each row's own entry
+        const int lo32 = (int)lo;
+        int self[kWRowsPerThread];
+#pragma unroll
+        for (int i = 0; i < kWRowsPerThread; ++i) {
+          self[i] = 4 * (int)(r0 + threadIdx.x + i * kWThreads - lo32);
+#pragma unroll
+          for (int q = 0; q < RMAX; ++q) col[i][q] = 4 * (col[i][q] - lo32);
+        }
+        int s = (int)(g % kWStages);
+        uint32_t ph = (uint32_t)((g / kWStages) & 1);
         for (int64_t b = 0; b < p; ++b, ++g) {
-          const int s = (int)(g % kWStages);
-          const uint32_t ph = (uint32_t)((g / kWStages) & 1);
           const bool ok = !*fail && mbar_wait_bounded(sp_smem(&sh->full[s]), ph, fail);
           if (!ok) {
             if (lane == 0) {
@@ -316,20 +321,27 @@ csr_spmm_window_kernel(const int32_t *__restrict__ rp, const int32_t *__restrict
             }
             break;
           }
-          const float *w = sh->win[s];
+          const char *w = reinterpret_cast<const char *>(sh->win[s]);
+          float *Wb = W + b * ldw + r0 + threadIdx.x;
 #pragma unroll
           for (int i = 0; i < kWRowsPerThread; ++i) {
-            const int lr = t + i * kWThreads;
-            if (lr < rows) {
-              float acc = shift * w[r0 + lr - lo];
-              const int f1 = sh->rp[lr + 1];
-              for (int e = sh->rp[lr]; e < f1; ++e) acc = fmaf(sh->val[e - a0], w[sh->ci[e - a0] - lo], acc);
-              W[b * ldw + r0 + lr] = acc;
+            if ((int)threadIdx.x + i * kWThreads < rows) {
+              float acc = shift * *reinterpret_cast<const float *>(w + self[i]);
+#pragma unroll
+              for (int q = 0; q < RMAX; ++q)
+                acc = fmaf(a[i][q], *reinterpret_cast<const float *>(w + col[i][q]), acc);
+              for (int e = e0[i] + RMAX; e < e0[i] + len[i]; ++e)
+                acc = fmaf(__ldg(val + e), *reinterpret_cast<const float *>(w + 4 * (__ldg(ci + e) - lo32)), acc);
+              Wb[i * kWThreads] = acc;
             }
           }
           __syncwarp();
           if (lane == 0)
             asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(sp_smem(&sh->empty[s])) : "memory");
+          if (++s == kWStages) {
+            s = 0;
+            ph ^= 1u;
+          }
         }
       }
       continue;
@@ -337,22 +349,20 @@ csr_spmm_window_kernel(const int32_t *__restrict__ rp, const int32_t *__restrict
 
     // gather path
     if (copier) continue;
-    auto col_at = [&](int64_t e) -> int64_t { return staged ? sh->ci[e - a0] : __ldg(ci + e); };
-    auto val_at = [&](int64_t e) -> float { return staged ? sh->val[e - a0] : __ldg(val + e); };
 #pragma unroll 1
     for (int i = 0; i < kWRowsPerThread; ++i) {
       const int lr = threadIdx.x + i * kWThreads;
       const bool has_row = lr < rows;
-      const int e0 = has_row ? sh->rp[lr] : 0, e1 = has_row ? sh->rp[lr + 1] : 0;
-      int len = e1 - e0;
+      int lmax = len[i];
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) len = max(len, __shfl_xor_sync(0xffffffffu, len, o));
-      if (len <= kWLong) {
+      for (int o = 16; o > 0; o >>= 1) lmax = max(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
+      if (lmax <= kWLong) {
         const int64_t r = r0 + lr;
         for (int64_t b = 0; b < p; ++b) {
           if (has_row) {
-            float acc = shift * __ldg(V + b * ldv + r);
-            for (int e = e0; e < e1; ++e) acc = fmaf(val_at(e), __ldg(V + b * ldv + col_at(e)), acc);
+            const float *Vb = V + b * ldv;
+            float acc = shift * __ldg(Vb + r);
+            for (int e = e0[i]; e < e0[i] + len[i]; ++e) acc = fmaf(__ldg(val + e), __ldg(Vb + __ldg(ci + e)), acc);
             W[b * ldw + r] = acc;
           }
         }
@@ -365,11 +375,12 @@ csr_spmm_window_kernel(const int32_t *__restrict__ rp, const int32_t *__restrict
         const int f0 = sh->rp[lj], f1 = sh->rp[lj + 1];
         const int64_t r = r0 + lj;
         for (int64_t b = 0; b < p; ++b) {
+          const float *Vb = V + b * ldv;
           float acc = 0.f;
-          for (int e = f0 + lane; e < f1; e += 32) acc = fmaf(val_at(e), __ldg(V + b * ldv + col_at(e)), acc);
+          for (int e = f0 + lane; e < f1; e += 32) acc = fmaf(__ldg(val + e), __ldg(Vb + __ldg(ci + e)), acc);
 #pragma unroll
           for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-          if (lane == 0) W[b * ldw + r] = fmaf(shift, __ldg(V + b * ldv + r), acc);
+          if (lane == 0) W[b * ldw + r] = fmaf(shift, __ldg(Vb + r), acc);
         }
       }
     }
@@ -382,32 +393,44 @@ csr_spmm_window_kernel(const int32_t *__restrict__ rp, const int32_t *__restrict
   }
 }
 
-int launch_csr_spmm(const int32_t *row_ptr, const int32_t *col_idx, const float *val, int64_t n,
-                    int64_t nnz, const float *V, int64_t ldv, float *W, int64_t ldw, int64_t p,
-                    double shift, int *status, cudaStream_t s) {
-  if (n <= 0 || p <= 0) return MFG_OK;
-  if (n > 0x7ffffff0 || ldv % 8 != 0 || reinterpret_cast<uintptr_t>(V) % 16 != 0) return MFG_ERR_UNSUPPORTED;
+template <int RMAX>
+static int launch_csr_spmm_t(const int32_t *row_ptr, const int32_t *col_idx, const float *val, int64_t n,
+                             const float *V, int64_t ldv, float *W, int64_t ldw, int64_t p, double shift,
+                             int *status, cudaStream_t s) {
   const size_t smem = sizeof(WinShared);
   static int per_sm = 0, sms = 0;
   if (per_sm == 0) {
     int dev = 0;
     MFG_CUDA_TRY(cudaGetDevice(&dev));
     MFG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    MFG_CUDA_TRY(cudaFuncSetAttribute(csr_spmm_window_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)smem));
+    MFG_CUDA_TRY(cudaFuncSetAttribute(csr_spmm_window_kernel<RMAX>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int q = 0;
-    MFG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&q, csr_spmm_window_kernel, kWThreads + 32, smem));
+    MFG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&q, csr_spmm_window_kernel<RMAX>,
+                                                               kWThreads + 32, smem));
     if (q < 1) return MFG_ERR_UNSUPPORTED;
     per_sm = q;
   }
-  const int64_t ntiles = ceil_div(n, kWRows);
-  int64_t grid = (int64_t)sms * per_sm;
-  if (grid > ntiles) grid = ntiles;
-  const int vec_ok = (reinterpret_cast<uintptr_t>(col_idx) % 16 == 0) &&
-                     (reinterpret_cast<uintptr_t>(val) % 16 == 0);
-  csr_spmm_window_kernel<<<(unsigned)grid, kWThreads + 32, smem, s>>>(
-      row_ptr, col_idx, val, n, nnz, vec_ok, V, ldv, W, ldw, p, (float)shift, status);
+  const int64_t G = (int64_t)sms * per_sm;
+  const int64_t tile_rows = kWRows;
+  const int64_t ntiles = ceil_div(n, tile_rows);
+  const int64_t grid = G < ntiles ? G : ntiles;
+  csr_spmm_window_kernel<RMAX><<<(unsigned)grid, kWThreads + 32, smem, s>>>(
+      row_ptr, col_idx, val, n, (int)tile_rows, V, ldv, W, ldw, p, (float)shift, status);
   return MFG_LAUNCH_STATUS();
+}
+
+int launch_csr_spmm(const int32_t *row_ptr, const int32_t *col_idx, const float *val, int64_t n,
+                    int64_t nnz, const float *V, int64_t ldv, float *W, int64_t ldw, int64_t p,
+                    double shift, int *status, cudaStream_t s) {
+  if (n <= 0 || p <= 0) return MFG_OK;
+  if (n > 0x7ffffff0 || ldv % 8 != 0 || reinterpret_cast<uintptr_t>(V) % 16 != 0) return MFG_ERR_UNSUPPORTED;
+  // entries held in registers per row: 6 covers 2-D 5-point stencils, 12 the
+  // 3-D 7-point ones and up to 12 entries; longer rows read the rest from
+  // global memory
+  if (nnz <= 6 * n)
+    return launch_csr_spmm_t<6>(row_ptr, col_idx, val, n, V, ldv, W, ldw, p, shift, status, s);
+  return launch_csr_spmm_t<12>(row_ptr, col_idx, val, n, V, ldv, W, ldw, p, shift, status, s);
 }
 
 // ---------------------------------------------------------------------------

@@ -1,8 +1,8 @@
 """The CSR SpMM kernel (csr_spmm_window_kernel) against scipy on every path:
 the streamed-window path (banded matrices), the gather path (wide column
-patterns), the warp-cooperative path for long rows, tiles whose CSR segment
-exceeds the staging buffer, ragged and empty rows, and CSR arrays whose base
-is not 16-byte aligned (no vector loads)."""
+patterns), the warp-cooperative path for long rows, rows longer than the
+entries held in registers, both register widths (6 and 12 entries), ragged
+and empty rows, and CSR arrays at unaligned offsets."""
 
 import numpy as np
 import pytest
@@ -24,7 +24,7 @@ def _check(A, p=5, shift=0.3, seed=0, op=None):
     np.testing.assert_allclose(got, want, rtol=1e-5, atol=1e-5 * np.abs(want).max())
 
 
-@pytest.mark.parametrize("case", ["laplace", "banded", "random", "long", "huge_segment", "empty_rows"])
+@pytest.mark.parametrize("case", ["laplace", "banded", "random", "long", "wide_rows", "dense_band", "empty_rows"])
 def test_csr_spmm_paths_match_scipy(case):
     rng = np.random.default_rng(7)
     if case == "laplace":
@@ -40,9 +40,12 @@ def test_csr_spmm_paths_match_scipy(case):
         lens = rng.integers(1, 4, size=n)
         lens[[5, 1130, 4100, 8999]] = [70, 2000, 33, 900]
         A = _random_csr(n, rng, lens)
-    elif case == "huge_segment":
+    elif case == "wide_rows":
         n = 3000
         A = _random_csr(n, rng, np.full(n, 40), band=1000)
+    elif case == "dense_band":
+        n = 20000
+        A = _random_csr(n, rng, rng.integers(6, 16, size=n), band=1000)  # 12 entries in registers
     else:
         n = 5000
         lens = rng.integers(0, 4, size=n)
