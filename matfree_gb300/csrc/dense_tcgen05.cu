@@ -42,7 +42,6 @@ constexpr int kRowBytes = kBK * 2;  // 64-byte rows -> SWIZZLE_64B (128 -> SWIZZ
 static_assert(kRowBytes == 64 || kRowBytes == 128, "supported swizzle widths");
 constexpr int kUmmaK = 16;          // K per tcgen05.mma of kind::f16
 constexpr int kGemmThreads = 192;
-constexpr int kChunkSlices = 128;   // pair form: K slices (of kBK) accumulated per chunk
 constexpr int64_t kPairMinRows = 1024;  // CTA pairs from this operator size on
 
 struct GemmShared {
@@ -50,8 +49,6 @@ struct GemmShared {
   uint64_t empty[8];
   uint64_t tmem_full;
   uint64_t drain;
-  uint64_t acc_full;   // pair form: a chunk's accumulator is complete
-  uint64_t acc_empty;  // pair form (lead CTA): the epilogues of both CTAs folded it in
   uint32_t tmem_base;
   int abort;
 };
@@ -80,34 +77,6 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volati
     if (status) atomicExch(status, (int)MFG_ERR_TIMEOUT);
   }
   return false;
-}
-
-// Bounded wait with cluster-scope acquire: for a barrier whose arrivals come
-// from the other CTA of the pair (release.cluster), ordering that CTA's TMEM
-// reads before this thread's next MMAs.
-__device__ __forceinline__ bool mbar_wait_cluster(uint64_t *bar, uint32_t parity, volatile int *abort_flag,
-                                                  int *status) {
-  const uint32_t saddr = smem_u32(bar);
-  const uint64_t t0 = global_ns();
-  for (uint32_t it = 0;; ++it) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}\n"
-        : "=r"(ok)
-        : "r"(saddr), "r"(parity)
-        : "memory");
-    if (ok) return true;
-    if ((it & 63u) == 63u) {
-      if (*abort_flag) return false;
-      if (global_ns() - t0 > kMbarWaitNs) {
-        *abort_flag = 1;
-        if (status) atomicExch(status, (int)MFG_ERR_TIMEOUT);
-        return false;
-      }
-    }
-  }
 }
 
 __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, uint64_t *bar, int x,
@@ -159,30 +128,6 @@ __device__ __forceinline__ void umma_commit(uint64_t *bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                    smem_u32(bar))
                : "memory");
-}
-
-__device__ __forceinline__ void tmem_st16(uint32_t taddr, const float (&v)[16]) {
-  asm volatile(
-      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "
-      "{%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16};"
-      ::"r"(taddr), "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
-        "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])),
-        "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7])), "r"(__float_as_uint(v[8])),
-        "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])), "r"(__float_as_uint(v[11])),
-        "r"(__float_as_uint(v[12])), "r"(__float_as_uint(v[13])), "r"(__float_as_uint(v[14])),
-        "r"(__float_as_uint(v[15]))
-      : "memory");
-}
-
-__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
-  uint32_t r[8];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
 }
 
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
@@ -418,18 +363,6 @@ __device__ __forceinline__ void umma_commit_pair_local(uint64_t *bar) {
                : "memory");
 }
 
-// Chunked accumulation.  The tensor pipe's fp32 accumulation into TMEM
-// truncates, so a long K sum into one accumulator drifts toward zero by an
-// amount that grows with the number of accumulation steps (measured: a
-// relative bias of about -3e-5 at K = 16384).  The pair form therefore
-// accumulates K in chunks of kChunkSlices slices: each chunk starts a fresh
-// accumulator (TMEM columns [0, cols)); the epilogue warps add it to the
-// running sum held in TMEM columns [cols, 2 cols) with fp32 rounding
-// (tcgen05.ld of both, add, tcgen05.st) and release the accumulator through
-// the lead CTA's acc_empty barrier before the MMAs of the next chunk start.
-// The last chunk is added to the running sum and the shift term on its way to
-// W.  The MMAs wait for each fold (a few microseconds per chunk of about
-// 60 microseconds at BN = 256).
 template <bool kSplit>
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kGemmThreads, 1)
 dense_tcgen05_pair_kernel(const __grid_constant__ CUtensorMap map_ahi,
@@ -457,8 +390,6 @@ dense_tcgen05_pair_kernel(const __grid_constant__ CUtensorMap map_ahi,
   const int num_k_all = (n + kBK - 1) / kBK;
   const int kb0 = (int)((int64_t)num_k_all * blockIdx.z / gridDim.z);
   const int num_k = (int)((int64_t)num_k_all * (blockIdx.z + 1) / gridDim.z) - kb0;
-  const int nchunks = (num_k + kChunkSlices - 1) / kChunkSlices;
-  const uint32_t run_col = tmem_cols / 2;  // running sum: TMEM columns [run_col, 2 run_col)
   const bool split_k = gridDim.z > 1;
   volatile int *abort_flag = &sh->abort;
 
@@ -467,9 +398,8 @@ dense_tcgen05_pair_kernel(const __grid_constant__ CUtensorMap map_ahi,
       mbar_init(&sh->full[s], 1);
       mbar_init(&sh->empty[s], 1);
     }
+    mbar_init(&sh->tmem_full, 1);
     mbar_init(&sh->drain, 1);
-    mbar_init(&sh->acc_full, 1);
-    mbar_init(&sh->acc_empty, 8);  // 4 epilogue warps in each CTA of the pair
     sh->abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -521,13 +451,6 @@ dense_tcgen05_pair_kernel(const __grid_constant__ CUtensorMap map_ahi,
       const uint32_t idesc = instr_desc_bf16(2 * kBM, BN);
       int done = 0;
       for (int kt = 0; kt < num_k; ++kt) {
-        const int ck = kt / kChunkSlices;
-        const int in_chunk = kt - ck * kChunkSlices;
-        if (in_chunk == 0 && ck >= 1) {
-          // both epilogues folded chunk ck - 1 into the running sum
-          if (!mbar_wait_cluster(&sh->acc_empty, (uint32_t)(ck - 1) & 1u, abort_flag, status)) break;
-          tc_fence_after();
-        }
         const int s = kt % stages;
         const uint32_t ph = (uint32_t)(kt / stages) & 1u;
         if (!mbar_wait(&sh->full[s], ph, abort_flag, status)) break;
@@ -538,7 +461,7 @@ dense_tcgen05_pair_kernel(const __grid_constant__ CUtensorMap map_ahi,
 #pragma unroll
         for (int kk = 0; kk < kBK / kUmmaK; ++kk) {
           const uint32_t off = (uint32_t)kk * kUmmaK * 2;
-          const uint32_t acc = (in_chunk > 0 || kk > 0) ? 1u : 0u;
+          const uint32_t acc = (kt > 0 || kk > 0) ? 1u : 0u;
           umma_bf16_pair(tmem, sw_desc(ahi + off), sw_desc(bhi + off), idesc, acc);
           if (kSplit) {
             umma_bf16_pair(tmem, sw_desc(ahi + off), sw_desc(blo + off), idesc, 1u);
@@ -546,10 +469,11 @@ dense_tcgen05_pair_kernel(const __grid_constant__ CUtensorMap map_ahi,
           }
         }
         umma_commit_pair(&sh->empty[s]);
-        if (in_chunk == kChunkSlices - 1 || kt == num_k - 1) umma_commit_pair(&sh->acc_full);
         ++done;
       }
-      if (done != num_k) {
+      if (done == num_k) {
+        umma_commit_pair(&sh->tmem_full);
+      } else {
         umma_commit_pair_local(&sh->drain);
         mbar_wait_bounded(smem_u32(&sh->drain), 0, nullptr, kMbarWaitNs / 8);
       }
@@ -558,11 +482,9 @@ dense_tcgen05_pair_kernel(const __grid_constant__ CUtensorMap map_ahi,
     // epilogue: warps 2..5 -> TMEM lane quarters 2, 3, 0, 1 of this CTA's rows
     const int quarter = warp & 3;
     const int m = m0 + quarter * 32 + lane;
-    const uint32_t lane_off = (uint32_t)(quarter * 32) << 16;
-    const uint32_t lead_empty = map_to_rank(smem_u32(&sh->acc_empty), 0);
     // The shift term's probe values (shift * V[b][m]) are loaded one group of
-    // 16 probes ahead of the last chunk's accumulator reads, the first group
-    // while the main loop runs, so their latency stays off the epilogue's path.
+    // 16 probes ahead of the accumulator reads, the first group while the
+    // main loop runs, so their latency stays off the epilogue's path.
     float sv[16], svn[16];
     auto load_shift = [&](int c, float(&dst)[16]) {
 #pragma unroll
@@ -573,26 +495,13 @@ dense_tcgen05_pair_kernel(const __grid_constant__ CUtensorMap map_ahi,
       }
     };
     load_shift(0, sv);
-    bool ok = true;
-    for (int ck = 0; ck < nchunks && ok; ++ck) {
-      ok = __all_sync(0xffffffffu, mbar_wait<true>(&sh->acc_full, (uint32_t)ck & 1u, abort_flag, status));
-      tc_fence_after();
-      if (!ok) break;
-      const bool last = ck == nchunks - 1;
+    const bool ok = __all_sync(0xffffffffu, mbar_wait<true>(&sh->tmem_full, 0, abort_flag, status));
+    tc_fence_after();
+    if (ok) {
       for (int c = 0; c < BN; c += 16) {
-        if (last && c + 16 < BN) load_shift(c + 16, svn);
+        if (c + 16 < BN) load_shift(c + 16, svn);
         float v[16];
-        tmem_ld16(tmem + lane_off + (uint32_t)c, v);
-        if (ck > 0) {
-          float u[16];
-          tmem_ld16(tmem + lane_off + run_col + (uint32_t)c, u);
-#pragma unroll
-          for (int j = 0; j < 16; ++j) v[j] = u[j] + v[j];
-        }
-        if (!last) {
-          tmem_st16(tmem + lane_off + run_col + (uint32_t)c, v);
-          continue;
-        }
+        tmem_ld16(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)c, v);
         if (m < n) {
 #pragma unroll
           for (int j = 0; j < 16; ++j) {
@@ -610,21 +519,12 @@ dense_tcgen05_pair_kernel(const __grid_constant__ CUtensorMap map_ahi,
 #pragma unroll
         for (int j = 0; j < 16; ++j) sv[j] = svn[j];
       }
-      if (!last) {
-        // the running sum is stored and the accumulator read: release it
-        asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
-        tc_fence_before();
-        __syncwarp();
-        if (lane == 0)
-          asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(lead_empty)
-                       : "memory");
-      }
     }
   }
   __syncwarp();
   tc_fence_before();
   // neither CTA releases its TMEM or shared memory while the pair's MMAs,
-  // copies, commits or remote arrivals may still reach it
+  // copies or commits may still reach it
   cluster_sync_all();
   if (warp == 1) {
     tc_fence_after();
@@ -969,13 +869,13 @@ int launch_dense_tcgen05(const __nv_bfloat16 *A_hi, const __nv_bfloat16 *A_lo, i
       MFG_CUDA_TRY(cudaFuncSetAttribute(dense_tcgen05_pair_kernel<true>,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       dense_tcgen05_pair_kernel<true><<<grid, kGemmThreads, smem, s>>>(
-          mahi, malo, mbhi, mblo, Vf, ldvf, W, ldw, (int)n, (int)p, BN, stages, 2 * cols,
+          mahi, malo, mbhi, mblo, Vf, ldvf, W, ldw, (int)n, (int)p, BN, stages, cols,
           (float)shift, status);
     } else {
       MFG_CUDA_TRY(cudaFuncSetAttribute(dense_tcgen05_pair_kernel<false>,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       dense_tcgen05_pair_kernel<false><<<grid, kGemmThreads, smem, s>>>(
-          mahi, malo, mbhi, mblo, Vf, ldvf, W, ldw, (int)n, (int)p, BN, stages, 2 * cols,
+          mahi, malo, mbhi, mblo, Vf, ldvf, W, ldw, (int)n, (int)p, BN, stages, cols,
           (float)shift, status);
     }
     return MFG_LAUNCH_STATUS();

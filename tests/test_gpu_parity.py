@@ -323,8 +323,8 @@ def test_funm_lanczos_sym_logm_vector():
                                  # one and two probe tiles, a probe tile of 64; the
                                  # first three also split K over two CTAs
                                  (1024, 256), (1500, 256), (2600, 300), (1300, 64), (1100, 40),
-                                 # K accumulated in chunks of 4096 folded in TMEM: two
-                                 # chunks, four chunks, and two per half of a split K
+                                 # long K (one TMEM accumulator over K = 16384) and a
+                                 # ragged split K over two CTAs
                                  (4608, 256), (16384, 256), (9000, 96),
                                  # GEMV form (p <= 8): ragged column tails, 5 and 8 probes
                                  (203, 1), (1001, 5), (4099, 8)])
@@ -400,20 +400,3 @@ def test_dlpack_inputs_give_the_torch_results():
     a = mf.RBFKernelOperator(_DLPackOnly(x), precision="fp32").dense()
     b = mf.RBFKernelOperator(x, precision="fp32").dense()
     assert torch.equal(a, b)
-
-
-def test_tensor_core_product_is_unbiased_at_long_k():
-    # The tensor pipe's fp32 accumulation truncates; the CTA-pair GEMM folds
-    # K in chunks of 4096 with rounding, so the signed relative error of a
-    # K = 16384 product stays at the level of one chunk (unchunked: -3e-5).
-    n, p = 16384, 256
-    x = problems.rbf_points(n, seed=0).astype(np.float32)
-    op = mf.RBFKernelOperator(_t(x, torch.float32), precision="bf16x3", tau=0.0)
-    A64 = op.dense()
-    g = torch.Generator(device=DEV).manual_seed(3)
-    V = torch.sign(torch.randn(p, n, device=DEV, generator=g)) / np.sqrt(n)
-    W = op.matmat(V).double()
-    Wx = V.double() @ A64.T
-    bias = float(((W - Wx) * torch.sign(Wx)).sum() / Wx.abs().sum())
-    assert abs(bias) < 1.2e-5, bias
-
