@@ -202,6 +202,15 @@ def gpu_arm(args):
     prob = build_problem(args.config)
     kind, n, k, p = prob["kind"], prob["n"], prob["k"], prob["p"]
     precision = args.precision
+    tuned = None
+    if precision in ("bf16", "bf16x3") and kind in ("rbf", "dense") and not args.no_autotune:
+        # the tensor-core product's tile configuration for this GPU (timed once
+        # per machine, outside the measured region, and cached)
+        from matfree_gb300 import tuning
+
+        rules = tuning.ensure(precision=precision)
+        tuned = next((r for r in rules if r["n_lo"] <= n <= r["n_hi"] and r["p_lo"] <= min(p, 256) <= r["p_hi"]),
+                     None)
     dev = torch.device("cuda", torch.cuda.current_device())
     key = mf.prng.prng_key(1 + rank)
 
@@ -374,7 +383,7 @@ def gpu_arm(args):
             plain[name] = {"solves_per_s": 2.0 / (time.perf_counter() - t_p), "values": pv}
         torch.backends.cuda.matmul.allow_tf32 = tf32
 
-    result = {"rank": rank, "world": world, "total_ms": total_ms, "step_ms": step_ms, "prof": prof,
+    result = {"rank": rank, "world": world, "total_ms": total_ms, "step_ms": step_ms, "prof": prof, "tuned": tuned,
               "clocks": clocks, "estimate": est, "e2e": e2e, "values": values, "key": key,
               "launches": launches, "plain": plain, "two_sweep_retries": retries[0]}
     return result, prob
@@ -791,7 +800,7 @@ def serve_arm(args):
     torch.cuda.set_device(0)
     reqs = serve.synthetic_stream(args.requests, rate=args.rate, seed=0)
     warm = serve.synthetic_stream(8, rate=1e6, seed=99)
-    srv = serve.SLQServer(slots=args.slots, budget_bytes=150e9, precision="bf16x3")
+    srv = serve.SLQServer(slots=args.slots, budget_bytes=150e9, precision="bf16x3", autotune=True)
     srv.run(warm, realtime=False)
     torch.cuda.synchronize()
     with ClockSampler(0) as clk:
@@ -846,7 +855,9 @@ def serve_arm(args):
                          "unit": "TFLOP/s", "frac": tflops / peaks["tensor_burst"], "traffic": None,
                          "peak_source": f"of {peaks['source']}",
                          "note": "algorithmic operator flops of the whole stream over its wall time"},
-            "clocks": clocks}
+            "clocks": clocks, "packed_solves": stats["packed_solves"],
+            "packed_requests": stats["packed_requests"],
+            "gemm_tuning_rules": sum(1 for r in (srv.tuning or []) if r["bn"] or r["split_k"])}
     print(json.dumps(line), flush=True)
 
 
@@ -898,6 +909,8 @@ def main():
     ap.add_argument("--precision", default="bf16x3", choices=["fp32", "bf16", "bf16x3", "fp64"])
     ap.add_argument("--cpu-probes", type=int, default=8)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the built-in tensor-core tile configuration")
     ap.add_argument("--no-other-configs", action="store_true",
                     help="report the headline configuration only")
     ap.add_argument("--no-plain-fp32", action="store_true",
@@ -944,6 +957,7 @@ def main():
         "estimate": res["estimate"], "roofline": rl, "gpu_launches": launches,
         "clocks": res["clocks"], "e2e": res["e2e"],
         "kernel_ms_per_step": {c: v["ms"] / args.steps for c, v in res["prof"].items()},
+        "gemm_tile": res["tuned"],
         "reortho": {"form": "two reads of the basis per step" if _two_sweep(args, prob)
                     else "three reads of the basis per step",
                     "retries": res["two_sweep_retries"]},

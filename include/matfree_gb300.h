@@ -173,6 +173,18 @@ MFG_API int mfg_hessenberg_adjoint_ex(const mfg_operator *op, int64_t k, int64_t
                                       const void *dr, const double *dc, void *Lambda, void *dv,
                                       void *workspace, size_t workspace_bytes, void *stream);
 
+/* Tile configuration of the bf16 / bf16x3 tensor-core operator product (the
+ * CTA-pair form, n >= 1024) for operators of n in [n_lo, n_hi] applied to
+ * p in [p_lo, p_hi] probe vectors: probe tiles of bn columns (a multiple of
+ * 32 in [64, 256]; narrower tiles give more tiles per operator and re-read it
+ * once per tile) and K split in split_k parts (1 or 2; 0 and bn = 0 keep the
+ * built-in choice).  The last matching rule applies; process-wide, at most
+ * 256 rules.  Written by matfree_gb300.tuning (an autotuner that times the
+ * candidates on the device); no counterpart in the reference. */
+MFG_API int mfg_gemm_tuning_add(int64_t n_lo, int64_t n_hi, int64_t p_lo, int64_t p_hi, int32_t bn,
+                                int32_t split_k);
+MFG_API int mfg_gemm_tuning_clear(void);
+
 /* out_b = sum_i coef[b][i] q_{b,i} for p Krylov bases Q (p*k rows of ld,
  * dtype MFG_F32/MFG_F64; coef p x k float64): the back-projection
  * Q^T (f(T) e1) of f(A) v by Lanczos (matfree/funm.py:142-146), batched.

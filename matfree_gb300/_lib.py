@@ -82,6 +82,8 @@ SIGNATURES = {
     "mfg_adjoint_workspace_bytes": (c_size_t, [POINTER(MfgOperator), c_int64, c_int64, c_int64]),
     "mfg_hessenberg_adjoint": (c_int, [POINTER(MfgOperator), c_int64, c_int64, c_int64, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
     "mfg_hessenberg_adjoint_ex": (c_int, [POINTER(MfgOperator), c_int64, c_int64, c_int64, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
+    "mfg_gemm_tuning_add": (c_int, [c_int64, c_int64, c_int64, c_int64, c_int32, c_int32]),
+    "mfg_gemm_tuning_clear": (c_int, []),
     "mfg_basis_combine": (c_int, [c_int32, c_int64, c_int64, c_int64, c_int64, c_void_p, c_void_p, c_void_p, c_void_p]),
     "mfg_operator_apply_noalloc": (c_int, [POINTER(MfgOperator), c_void_p, c_void_p, c_int64, c_int64, c_void_p]),
     "mfg_operator_apply_noalloc_status": (c_int, [c_void_p]),

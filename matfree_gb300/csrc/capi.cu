@@ -1162,6 +1162,13 @@ int mfg_hessenberg_adjoint(const mfg_operator *op, int64_t k, int64_t p, int64_t
                                    Lambda, dv, workspace, workspace_bytes, stream);
 }
 
+int mfg_gemm_tuning_add(int64_t n_lo, int64_t n_hi, int64_t p_lo, int64_t p_hi, int32_t bn,
+                        int32_t split_k) {
+  return gemm_rule_add(n_lo, n_hi, p_lo, p_hi, bn, split_k);
+}
+
+int mfg_gemm_tuning_clear(void) { return gemm_rules_clear(); }
+
 int mfg_basis_combine(int32_t dtype, int64_t k, int64_t p, int64_t n, int64_t ld, const void *Q,
                       const double *coef, void *out, void *stream) {
   if (k < 0 || p < 0 || n <= 0 || ld < n || ld % 8 != 0) return MFG_ERR_BAD_ARG;

@@ -806,6 +806,45 @@ static int launch_dense_gemv(const __nv_bfloat16 *A_hi, const __nv_bfloat16 *A_l
   return MFG_LAUNCH_STATUS();
 }
 
+// ---------------------------------------------------------------------------
+// Tile configuration rules (set by the autotuner through mfg_gemm_tuning_add):
+// for operators of n in [n_lo, n_hi] applied to p in [p_lo, p_hi] probes, the
+// CTA-pair form uses probe tiles of `bn` columns and splits K in `split`
+// parts (0: the built-in choice).  The last matching rule wins.
+// ---------------------------------------------------------------------------
+struct GemmRule {
+  int64_t n_lo, n_hi, p_lo, p_hi;
+  int bn, split;
+};
+static std::mutex g_rules_mu;
+static GemmRule g_rules[256];
+static int g_nrules = 0;
+
+int gemm_rule_add(int64_t n_lo, int64_t n_hi, int64_t p_lo, int64_t p_hi, int bn, int split) {
+  if (n_lo > n_hi || p_lo > p_hi) return MFG_ERR_BAD_ARG;
+  if (bn != 0 && (bn < 64 || bn > 256 || bn % 32 != 0)) return MFG_ERR_BAD_ARG;
+  if (split < 0 || split > 2) return MFG_ERR_BAD_ARG;
+  std::lock_guard<std::mutex> lk(g_rules_mu);
+  if (g_nrules >= 256) return MFG_ERR_SCRATCH_LIMIT;
+  g_rules[g_nrules++] = GemmRule{n_lo, n_hi, p_lo, p_hi, bn, split};
+  return MFG_OK;
+}
+
+int gemm_rules_clear() {
+  std::lock_guard<std::mutex> lk(g_rules_mu);
+  g_nrules = 0;
+  return MFG_OK;
+}
+
+static GemmRule gemm_rule_for(int64_t n, int64_t p) {
+  std::lock_guard<std::mutex> lk(g_rules_mu);
+  for (int i = g_nrules - 1; i >= 0; --i) {
+    const GemmRule &r = g_rules[i];
+    if (n >= r.n_lo && n <= r.n_hi && p >= r.p_lo && p <= r.p_hi) return r;
+  }
+  return GemmRule{0, 0, 0, 0, 0, 0};
+}
+
 int launch_dense_tcgen05(const __nv_bfloat16 *A_hi, const __nv_bfloat16 *A_lo, int64_t lda,
                          const __nv_bfloat16 *V_hi, const __nv_bfloat16 *V_lo, int64_t ldvb,
                          const float *Vf, int64_t ldvf, float *W, int64_t ldw, int64_t n, int64_t p,
@@ -819,8 +858,10 @@ int launch_dense_tcgen05(const __nv_bfloat16 *A_hi, const __nv_bfloat16 *A_lo, i
   if (p <= kGemvMaxP)
     return launch_dense_gemv(A_hi, A_lo, lda, V_hi, V_lo, ldvb, Vf, ldvf, W, ldw, n, p, shift, s);
   // probes per tile: a multiple of 16 in [16, 256]
+  const GemmRule rule = n >= kPairMinRows ? gemm_rule_for(n, p) : GemmRule{0, 0, 0, 0, 0, 0};
   const int64_t pt = p < 256 ? p : 256;
-  const int BN = (int)((pt + 15) / 16 * 16);
+  int BN = (int)((pt + 15) / 16 * 16);
+  if (rule.bn > 0 && rule.bn < BN) BN = rule.bn;  // a narrower probe tile: more tiles per operator
   uint32_t cols = 32;
   while ((int)cols < BN) cols <<= 1;
   // CTA pairs (2-SM MMAs, M = 256) once the operator spans several pair tiles
@@ -860,7 +901,9 @@ int launch_dense_tcgen05(const __nv_bfloat16 *A_hi, const __nv_bfloat16 *A_lo, i
         sms = 152;
     }
     const int num_k_all = (int)((n + kBK - 1) / kBK);
-    if ((int64_t)grid.x * grid.y * 5 < (int64_t)sms * 3 && num_k_all >= 4 * stages) {
+    const bool split_default = (int64_t)grid.x * grid.y * 5 < (int64_t)sms * 3;
+    const bool split_k = rule.split == 0 ? split_default : rule.split == 2;
+    if (split_k && num_k_all >= 4 * stages) {
       grid.z = 2;
       MFG_CUDA_TRY(cudaMemset2DAsync(W, (size_t)ldw * sizeof(float), 0, (size_t)n * sizeof(float),
                                      (size_t)p, s));

@@ -91,6 +91,8 @@ template <typename T>
 int launch_adj_lincomb(const T *U, const T *lam, const T *R, const T *dq, int64_t dq_bstride,
                        const double *scal, int64_t n, int64_t ld, int64_t p, T *out, cudaStream_t s);
 int launch_axpy_f64(double a, const double *x, double *y, int64_t m, cudaStream_t s);
+int gemm_rule_add(int64_t n_lo, int64_t n_hi, int64_t p_lo, int64_t p_hi, int bn, int split);
+int gemm_rules_clear();
 template <typename T>
 int launch_basis_combine(const T *Q, int64_t k, int64_t ld, int64_t n, int64_t p, const double *coef,
                          T *out, cudaStream_t s);

@@ -400,3 +400,43 @@ def test_dlpack_inputs_give_the_torch_results():
     a = mf.RBFKernelOperator(_DLPackOnly(x), precision="fp32").dense()
     b = mf.RBFKernelOperator(x, precision="fp32").dense()
     assert torch.equal(a, b)
+
+
+@pytest.mark.parametrize("bn,split", [(128, 1), (64, 1), (128, 2), (0, 2), (0, 1)])
+def test_tensor_core_apply_under_tile_rules(bn, split):
+    # every tile configuration the autotuner may install gives the same product
+    from matfree_gb300 import _lib
+
+    n, p = 4608, 256
+    rng = np.random.default_rng(17)
+    A = rng.standard_normal((n, n)) / np.sqrt(n)
+    V = rng.standard_normal((p, n))
+    lib = _lib.lib()
+    try:
+        assert lib.mfg_gemm_tuning_add(n, n, p, p, bn, split) == 0
+        op = mf.DenseOperator(_t(A, torch.float32), precision="bf16x3", shift=0.5)
+        W = op.matmat(_t(V, torch.float32)).double().cpu().numpy()
+    finally:
+        lib.mfg_gemm_tuning_clear()
+    A32 = A.astype(np.float32).astype(np.float64)
+    V32 = V.astype(np.float32).astype(np.float64)
+    want = V32 @ A32.T + 0.5 * V32
+    assert np.abs(W - want).max() / np.abs(want).max() < 5e-5
+
+
+def test_autotuner_installs_rules_that_keep_the_product():
+    from matfree_gb300 import _lib, tuning
+
+    try:
+        rules = tuning.autotune(ns=(1024, 2048), ps=(64, 256), reps=1)
+        assert len(rules) == 4
+        assert all(r["ms"] <= r["default_ms"] + 1e-9 for r in rules)
+        n, p = 2048, 256
+        rng = np.random.default_rng(3)
+        A = rng.standard_normal((n, n)) / np.sqrt(n)
+        V = rng.standard_normal((p, n))
+        W = mf.DenseOperator(_t(A, torch.float32), precision="bf16x3").matmat(_t(V, torch.float32))
+        want = V.astype(np.float32).astype(np.float64) @ A.astype(np.float32).astype(np.float64).T
+        assert np.abs(W.double().cpu().numpy() - want).max() / np.abs(want).max() < 5e-5
+    finally:
+        _lib.lib().mfg_gemm_tuning_clear()

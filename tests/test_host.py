@@ -229,3 +229,24 @@ def test_host_arrays_and_unknown_objects_are_rejected():
         require_cuda(np.zeros(3), "x")  # a DLPack producer, but host memory
     with pytest.raises(TypeError, match="DLPack"):
         require_cuda([1.0, 2.0], "x")
+
+
+def test_tuning_rule_ranges_tile_the_axis():
+    from matfree_gb300 import tuning
+
+    ns = tuning.DEFAULT_NS
+    spans = [tuning._bounds(ns, i) for i in range(len(ns))]
+    assert spans[0][0] == 0 and spans[-1][1] >= 1 << 40
+    for (lo, hi), n in zip(spans, ns):
+        assert lo <= n <= hi
+    for (_, hi), (lo, _) in zip(spans, spans[1:]):
+        assert lo == hi + 1
+
+
+def test_gemm_tuning_rejects_bad_rules():
+    lib = _lib.lib()
+    assert lib.mfg_gemm_tuning_add(1024, 2048, 64, 64, 48, 0) == _lib.MFG_ERR_BAD_ARG  # not a multiple of 32
+    assert lib.mfg_gemm_tuning_add(1024, 2048, 64, 64, 128, 3) == _lib.MFG_ERR_BAD_ARG
+    assert lib.mfg_gemm_tuning_add(2048, 1024, 64, 64, 128, 1) == _lib.MFG_ERR_BAD_ARG
+    assert lib.mfg_gemm_tuning_add(1024, 2048, 64, 64, 128, 1) == _lib.MFG_OK
+    assert lib.mfg_gemm_tuning_clear() == _lib.MFG_OK
