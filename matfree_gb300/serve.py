@@ -104,7 +104,28 @@ def _flags(k: int, precision: str) -> int:
 class _Slot:
     stream: torch.cuda.Stream
     workspace: Workspace = field(default_factory=Workspace)
+    opbuf: Workspace = field(default_factory=Workspace)  # operator storage, reused by the slot
     busy: bool = False
+
+
+def _operator_views(slot: _Slot, members_n: int, n: int, ld: int, precision: str, device):
+    """Storage for `members_n` operators of n x ld entries in the slot's own
+    grow-only buffer: requests of every size reuse the same device memory, so
+    a long stream of mixed sizes does not fragment the allocator's cache (a
+    fragmented cache ends in allocation retries that synchronise the device)."""
+    es = {"bf16x3": 2, "bf16": 2, "fp32": 4, "fp64": 8}[precision]
+    arrays = 2 if precision == "bf16x3" else 1
+    one = n * ld * es
+    slot.opbuf.get(members_n * arrays * one, device)
+    buf = slot.opbuf.buf
+    dt = {"bf16x3": torch.bfloat16, "bf16": torch.bfloat16, "fp32": torch.float32, "fp64": torch.float64}[precision]
+    out = []
+    for m in range(members_n):
+        base = m * arrays * one
+        a = buf[base:base + one].view(dt).view(n, ld)
+        a_lo = buf[base + one:base + 2 * one].view(dt).view(n, ld) if arrays == 2 else None
+        out.append((a, a_lo))
+    return out
 
 
 class _GroupOperator:
@@ -204,7 +225,13 @@ class SLQServer:
         with torch.cuda.stream(slot.stream):
             xh = torch.from_numpy(np.ascontiguousarray(req.x, dtype=np.float32)).pin_memory()
             xd = xh.to(self.device, non_blocking=True)
-            op = RBFKernelOperator(xd, s2=req.s2, ell=req.ell, tau=req.tau, precision=self.precision)
+            ((a, a_lo),) = _operator_views(slot, 1, n, ld, self.precision, self.device)
+            st = lib.mfg_rbf_build(ctypes.c_void_p(xd.data_ptr()), n, 3, req.s2, req.ell,
+                                   _lib.PRECISIONS[self.precision], ctypes.c_void_p(a.data_ptr()),
+                                   ctypes.c_void_p(a_lo.data_ptr() if a_lo is not None else 0), ld,
+                                   ctypes.c_void_p(slot.stream.cuda_stream))
+            _lib.check(st, "mfg_rbf_build")
+            op = DenseOperator._from_storage(n, self.precision, a, a_lo, req.tau)
             probes = torch.zeros((req.p, ld), dtype=op.basis_dtype, device=self.device)
             key = np.ascontiguousarray(np.asarray(req.key, dtype=np.uint32).reshape(2))
             st = lib.mfg_sampler_signs(key.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), req.p, n, ld,
@@ -245,13 +272,15 @@ class SLQServer:
         with torch.cuda.stream(slot.stream):
             ops = []
             panel = torch.zeros((P, ld), dtype=torch.float32, device=self.device)
-            for r, b0 in zip(members, starts):
+            views = _operator_views(slot, len(members), n, ld, self.precision, self.device)
+            for r, b0, (a, a_lo) in zip(members, starts, views):
                 nr = r.x.shape[0]
                 xh = torch.from_numpy(np.ascontiguousarray(r.x, dtype=np.float32)).pin_memory()
                 xd = xh.to(self.device, non_blocking=True)
-                dt = torch.float32 if self.precision == "fp32" else torch.bfloat16
-                a = torch.zeros((n, ld), dtype=dt, device=self.device)
-                a_lo = torch.zeros((n, ld), dtype=dt, device=self.device) if self.precision == "bf16x3" else None
+                # rows nr..n-1 of the padded operator are zero (the builder writes rows < nr)
+                a[nr:].zero_()
+                if a_lo is not None:
+                    a_lo[nr:].zero_()
                 st = lib.mfg_rbf_build(ctypes.c_void_p(xd.data_ptr()), nr, 3, r.s2, r.ell,
                                        _lib.PRECISIONS[self.precision], ctypes.c_void_p(a.data_ptr()),
                                        ctypes.c_void_p(a_lo.data_ptr() if a_lo is not None else 0), ld,
