@@ -902,7 +902,9 @@ def main():
     ap.add_argument("--requests", type=int, default=10000)
     ap.add_argument("--baseline-requests", type=int, default=200,
                     help="requests of the plain fp32 comparison (0: all of them)")
-    ap.add_argument("--rate", type=float, default=100.0)
+    ap.add_argument("--rate", type=float, default=150.0,
+                    help="Poisson arrival rate of the serving stream (above the server's capacity, so "
+                         "that solves/s measures the capacity and latencies include queueing)")
     ap.add_argument("--slots", type=int, default=8)
     ap.add_argument("--inflight", type=int, default=3,
                     help="independent solves in flight (round-robin over CUDA streams)")
