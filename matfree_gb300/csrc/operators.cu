@@ -21,12 +21,20 @@ template <> struct SimtCfg<float> {
 template <> struct SimtCfg<double> {
   static constexpr int BM = 128, BP = 64, BK = 8, TM = 8, TP = 4;
 };
+// Small tiles for operators whose large-tile grid would not fill the GPU
+// (e.g. n = 1000, p = 100: 16 CTAs of 128 x 64 against 128 of 32 x 32).
+template <typename T> struct SimtCfgSmall;
+template <> struct SimtCfgSmall<float> {
+  static constexpr int BM = 32, BP = 32, BK = 32, TM = 2, TP = 2;
+};
+template <> struct SimtCfgSmall<double> {
+  static constexpr int BM = 32, BP = 32, BK = 16, TM = 2, TP = 2;
+};
 
-template <typename T>
+template <typename T, typename C>
 __global__ void __launch_bounds__(256)
 dense_simt_kernel(const T *__restrict__ A, int64_t lda, const T *__restrict__ V, int64_t ldv,
                   T *__restrict__ W, int64_t ldw, int64_t n, int64_t p, T shift) {
-  using C = SimtCfg<T>;
   constexpr int BM = C::BM, BP = C::BP, BK = C::BK, TM = C::TM, TP = C::TP;
   constexpr int VW = Vec<T>::width;
   using VT = typename Vec<T>::type;
@@ -102,10 +110,17 @@ dense_simt_kernel(const T *__restrict__ A, int64_t lda, const T *__restrict__ V,
 #pragma unroll
     for (int kk = 0; kk < BK; ++kk) {
       T a[TM], v[TP];
+      if constexpr (TM % VW == 0 && TP % VW == 0) {
 #pragma unroll
-      for (int i = 0; i < TM; i += VW) vec_to_array<T>(*reinterpret_cast<const VT *>(&As[kk][tx * TM + i]), a + i);
+        for (int i = 0; i < TM; i += VW) vec_to_array<T>(*reinterpret_cast<const VT *>(&As[kk][tx * TM + i]), a + i);
 #pragma unroll
-      for (int j = 0; j < TP; j += VW) vec_to_array<T>(*reinterpret_cast<const VT *>(&Vs[kk][ty * TP + j]), v + j);
+        for (int j = 0; j < TP; j += VW) vec_to_array<T>(*reinterpret_cast<const VT *>(&Vs[kk][ty * TP + j]), v + j);
+      } else {  // thread tiles narrower than a 16-byte vector
+#pragma unroll
+        for (int i = 0; i < TM; ++i) a[i] = As[kk][tx * TM + i];
+#pragma unroll
+        for (int j = 0; j < TP; ++j) v[j] = Vs[kk][ty * TP + j];
+      }
 #pragma unroll
       for (int i = 0; i < TM; ++i)
 #pragma unroll
@@ -130,11 +145,26 @@ template <typename T>
 int launch_dense_simt(const T *A, int64_t lda, const T *V, int64_t ldv, T *W, int64_t ldw,
                       int64_t n, int64_t p, double shift, cudaStream_t s) {
   using C = SimtCfg<T>;
+  using CS = SimtCfgSmall<T>;
   if (n <= 0 || p <= 0) return MFG_OK;
-  const int64_t gy = ceil_div(p, C::BP);
+  static int sms = 0;
+  if (sms == 0) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      sms = 152;
+  }
+  const int64_t gx = ceil_div(n, C::BM), gy = ceil_div(p, C::BP);
+  if (gx * gy < sms) {
+    const int64_t sy = ceil_div(p, CS::BP);
+    if (sy > 65535) return MFG_ERR_UNSUPPORTED;
+    dim3 grid((unsigned)ceil_div(n, CS::BM), (unsigned)sy);
+    dense_simt_kernel<T, CS><<<grid, 256, 0, s>>>(A, lda, V, ldv, W, ldw, n, p, (T)shift);
+    return MFG_LAUNCH_STATUS();
+  }
   if (gy > 65535) return MFG_ERR_UNSUPPORTED;
-  dim3 grid((unsigned)ceil_div(n, C::BM), (unsigned)gy);
-  dense_simt_kernel<T><<<grid, 256, 0, s>>>(A, lda, V, ldv, W, ldw, n, p, (T)shift);
+  dim3 grid((unsigned)gx, (unsigned)gy);
+  dense_simt_kernel<T, C><<<grid, 256, 0, s>>>(A, lda, V, ldv, W, ldw, n, p, (T)shift);
   return MFG_LAUNCH_STATUS();
 }
 template int launch_dense_simt<float>(const float *, int64_t, const float *, int64_t, float *,
