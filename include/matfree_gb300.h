@@ -177,13 +177,27 @@ MFG_API int mfg_hessenberg_adjoint_ex(const mfg_operator *op, int64_t k, int64_t
  * CTA-pair form, n >= 1024) for operators of n in [n_lo, n_hi] applied to
  * p in [p_lo, p_hi] probe vectors: probe tiles of bn columns (a multiple of
  * 32 in [64, 256]; narrower tiles give more tiles per operator and re-read it
- * once per tile) and K split in split_k parts (1 or 2; 0 and bn = 0 keep the
- * built-in choice).  The last matching rule applies; process-wide, at most
+ * once per tile) and the form split_k: 1 one tile per CTA pair, 2 K split in
+ * two halves on twice the pairs, 3 persistent pairs (one per two SMs) that
+ * spread the last wave of tiles over every SM by splitting each of its tiles
+ * once along K (0 and bn = 0 keep the built-in choice).  Split tiles add two
+ * partial products into a zeroed output, which does not depend on timing.  The last matching rule applies; process-wide, at most
  * 256 rules.  Written by matfree_gb300.tuning (an autotuner that times the
  * candidates on the device); no counterpart in the reference. */
 MFG_API int mfg_gemm_tuning_add(int64_t n_lo, int64_t n_hi, int64_t p_lo, int64_t p_hi, int32_t bn,
                                 int32_t split_k);
 MFG_API int mfg_gemm_tuning_clear(void);
+
+/* Work list of the persistent CTA-pair form (mfg_gemm_tuning_add split_k =
+ * 3) of an n x n operator applied to p probes with probe tiles of bn columns
+ * on at most max_pairs CTA pairs (half the SMs), K tails shorter than
+ * min_tail slices of 32 not split off (the product uses its ring depth).
+ * Writes up to `capacity` items of four int32 (pair, tile, first K slice,
+ * end K slice) in the order each pair runs them, tiles numbered row tile
+ * (256 rows) first; returns the number of items, or minus an error code.
+ * Host only (no device call): for inspecting and testing the schedule. */
+MFG_API int64_t mfg_gemm_pair_schedule(int64_t n, int64_t p, int32_t bn, int32_t max_pairs,
+                                       int32_t min_tail, int32_t *items, int64_t capacity);
 
 /* out_b = sum_i coef[b][i] q_{b,i} for p Krylov bases Q (p*k rows of ld,
  * dtype MFG_F32/MFG_F64; coef p x k float64): the back-projection
@@ -376,6 +390,19 @@ MFG_API int mfg_operator_apply_noalloc(const mfg_operator *op, const void *V, vo
  * mfg_operator_apply_noalloc on the current device (MFG_OK or
  * MFG_ERR_TIMEOUT), or a host error code.  Allocates nothing. */
 MFG_API int mfg_operator_apply_noalloc_status(void *stream);
+
+/* Self-test of the bounded device-side waits that every kernel of this
+ * library uses (failure detection without a GPU fault).  One CTA waits on an
+ * mbarrier that nothing arrives on: warp 0 polls for `limit_ns`, gives up,
+ * raises the CTA's failure flag and writes MFG_ERR_TIMEOUT to *status (a
+ * device int32 the caller zeroes); warp 1 sleeps in the wait with the
+ * production limit (2 s) and leaves early through the failure flag.  `times`
+ * (device, 5 x uint64) receives: warp 0's wait in ns, whether it completed
+ * (0), warp 1's wait in ns, whether it completed (0), the final flag (1).
+ * No copy is in flight and no tensor memory is held, so the context stays
+ * usable; the return code reports launch errors only.  No reference
+ * counterpart: matfree's JAX code has no device-side waits. */
+MFG_API int mfg_wait_selftest(uint64_t limit_ns, void *status, void *times, void *stream);
 
 #ifdef __cplusplus
 }

@@ -87,6 +87,8 @@ SIGNATURES = {
     "mfg_basis_combine": (c_int, [c_int32, c_int64, c_int64, c_int64, c_int64, c_void_p, c_void_p, c_void_p, c_void_p]),
     "mfg_operator_apply_noalloc": (c_int, [POINTER(MfgOperator), c_void_p, c_void_p, c_int64, c_int64, c_void_p]),
     "mfg_operator_apply_noalloc_status": (c_int, [c_void_p]),
+    "mfg_wait_selftest": (c_int, [ctypes.c_uint64, c_void_p, c_void_p, c_void_p]),
+    "mfg_gemm_pair_schedule": (c_int64, [c_int64, c_int64, c_int32, c_int32, c_int32, c_void_p, c_int64]),
     "mfg_profile_enable": (c_int, [c_int]),
     "mfg_profile_read": (c_int, [c_int32, POINTER(c_double), POINTER(c_double), POINTER(c_double), POINTER(c_int64)]),
 }

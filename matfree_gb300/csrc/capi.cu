@@ -1102,6 +1102,13 @@ int mfg_operator_apply_noalloc_status(void *stream) {
   return word;
 }
 
+int mfg_wait_selftest(uint64_t limit_ns, void *status, void *times, void *stream) {
+  if (!status || !times) return MFG_ERR_BAD_ARG;
+  if (limit_ns == 0 || limit_ns > kMbarWaitNs) return MFG_ERR_BAD_ARG;
+  return launch_wait_selftest(limit_ns, static_cast<int *>(status),
+                              static_cast<unsigned long long *>(times), as_stream(stream));
+}
+
 int mfg_hessenberg(const mfg_operator *op, int64_t k, int64_t p, const void *V, int64_t ld,
                    int32_t reortho, void *Q, double *H, void *residual, double *init_len_inv,
                    void *workspace, size_t workspace_bytes, void *stream) {

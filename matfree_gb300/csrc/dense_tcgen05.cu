@@ -534,6 +534,278 @@ dense_tcgen05_pair_kernel(const __grid_constant__ CUtensorMap map_ahi,
 }
 
 // ---------------------------------------------------------------------------
+// Persistent 2-SM form: one CTA pair per pair of SMs, each working through a
+// fixed list of K ranges of output tiles, so that the last wave of tiles is
+// spread over every SM instead of leaving some of them idle (n = 16384,
+// 256 probes: 64 tiles on 76 pairs).
+//
+// Tiles are numbered row tile first (t = probe tile * tiles_m + row tile).
+// Pair q works, in order, on
+//   * the full tiles q, q + P, ..., q + (F - 1) P (the full waves), then
+//   * of the R = T - F P remainder tiles, either the main K range [0, Km) of
+//     tile F P + q (q < R), or the tail K range [Km, K) of the remainder
+//     tiles e, e + (P - R), e + 2 (P - R), ... (e = q - R).
+// Km balances the main piece against the c = ceil(R / (P - R)) tails of the
+// busiest spare pair.  A split tile thus has exactly two partial products,
+// which add into a zeroed W: a two-term sum is the same in either order, so
+// the result does not depend on timing.  The piece that starts at K = 0
+// adds the shift term.
+//
+// Two TMEM accumulators (2 x BN columns) alternate between work items: the
+// MMAs of item i + 1 run while the epilogue drains item i.  The epilogue
+// warps of both CTAs release an accumulator by arriving on the lead CTA's
+// "tmem_empty" barrier of that buffer (8 arrivals).
+// ---------------------------------------------------------------------------
+
+struct PairSchedule {
+  int tiles_m;  // 256-row tiles per probe tile
+  int P;        // CTA pairs of the grid
+  int F;        // full waves
+  int R;        // remainder tiles (main + tail pieces)
+  int Km;       // K slices of a main piece; >= K: remainder tiles not split
+};
+
+// Work item i of pair q: tile and K-slice range [kb, ke); false past the end.
+__host__ __device__ inline bool pair_item(const PairSchedule &sc, int K, int q, int i, int &tile,
+                                          int &kb, int &ke) {
+  if (i < sc.F) {
+    tile = q + i * sc.P;
+    kb = 0;
+    ke = K;
+    return true;
+  }
+  if (sc.R == 0) return false;
+  const int j = i - sc.F;
+  const int base = sc.F * sc.P;
+  if (q < sc.R) {
+    if (j > 0) return false;
+    tile = base + q;
+    kb = 0;
+    ke = sc.Km < K ? sc.Km : K;
+    return true;
+  }
+  if (sc.Km >= K) return false;
+  const int r = (q - sc.R) + j * (sc.P - sc.R);
+  if (r >= sc.R) return false;
+  tile = base + r;
+  kb = sc.Km;
+  ke = K;
+  return true;
+}
+
+struct GemmSharedP {
+  uint64_t full[8];
+  uint64_t empty[8];
+  uint64_t tmem_full[2];
+  uint64_t tmem_empty[2];
+  uint64_t drain;
+  uint32_t tmem_base;
+  int abort;
+};
+
+template <bool kSplit>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kGemmThreads, 1)
+dense_tcgen05_pair_persistent_kernel(const __grid_constant__ CUtensorMap map_ahi,
+                                     const __grid_constant__ CUtensorMap map_alo,
+                                     const __grid_constant__ CUtensorMap map_bhi,
+                                     const __grid_constant__ CUtensorMap map_blo,
+                                     const float *__restrict__ Vf, int64_t ldvf,
+                                     float *__restrict__ W, int64_t ldw, int n, int p, int BN,
+                                     int stages, uint32_t acc_cols, PairSchedule sc, float shift,
+                                     int *status) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t *tiles = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+  const uint32_t a_bytes = kBM * kBK * 2;
+  const uint32_t b_bytes = (uint32_t)(BN / 2) * kBK * 2;
+  const uint32_t stage_bytes = (kSplit ? 2u : 1u) * (a_bytes + b_bytes);
+  GemmSharedP *sh = reinterpret_cast<GemmSharedP *>(tiles + (size_t)stages * stage_bytes);
+
+  const uint32_t rank = cluster_rank();
+  const bool lead = rank == 0;
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const int q = (int)(blockIdx.x >> 1);
+  const int K = (n + kBK - 1) / kBK;
+  volatile int *abort_flag = &sh->abort;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < stages; ++s) {
+      mbar_init(&sh->full[s], 1);
+      mbar_init(&sh->empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&sh->tmem_full[b], 1);
+      mbar_init(&sh->tmem_empty[b], 8);  // 4 epilogue warps x 2 CTAs
+    }
+    mbar_init(&sh->drain, 1);
+    sh->abort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&sh->tmem_base)),
+                 "r"(2u * acc_cols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  cluster_sync_all();
+  tc_fence_after();
+  const uint32_t tmem = sh->tmem_base;
+  const uint32_t full0_lead = map_to_rank(smem_u32(&sh->full[0]), 0);
+
+  if (warp == 0) {
+    if (lane == 0) {
+      int g = 0;  // K slices issued over all items: the ring position
+      bool stop = false;
+      int tile, kb, ke;
+      for (int i = 0; !stop && pair_item(sc, K, q, i, tile, kb, ke); ++i) {
+        const int rt = tile % sc.tiles_m, ct = tile / sc.tiles_m;
+        const int m0 = rt * (2 * kBM) + (int)rank * kBM;
+        const int bh = ct * BN + (int)rank * (BN / 2);
+        for (int kt = kb; kt < ke; ++kt) {
+          const int s = g % stages;
+          const uint32_t ph = (uint32_t)(g / stages) & 1u;
+          if (!mbar_wait(&sh->empty[s], ph ^ 1u, abort_flag, status)) {
+            stop = true;
+            break;
+          }
+          uint8_t *st = tiles + (size_t)s * stage_bytes;
+          const uint32_t full_s = full0_lead + (uint32_t)(s * sizeof(uint64_t));
+          if (lead) mbar_arrive_expect_tx(&sh->full[s], 2u * stage_bytes);
+          const int kx = kt * kBK;
+          tma_load_2d_pair(st, &map_ahi, full_s, kx, m0);
+          tma_load_2d_pair(st + a_bytes, &map_bhi, full_s, kx, bh);
+          if (kSplit) {
+            tma_load_2d_pair(st + a_bytes + b_bytes, &map_alo, full_s, kx, m0);
+            tma_load_2d_pair(st + 2 * a_bytes + b_bytes, &map_blo, full_s, kx, bh);
+          }
+          ++g;
+        }
+      }
+      // drain (lead CTA): the copies of both CTAs complete on its "full" barriers
+      if (*abort_flag && lead) {
+        for (int t = (g > stages ? g - stages : 0); t < g; ++t) {
+          const int s = t % stages;
+          const uint32_t ph = (uint32_t)(t / stages) & 1u;
+          mbar_wait_bounded(smem_u32(&sh->full[s]), ph, nullptr, kMbarWaitNs / 8);
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0 && lead) {
+      const uint32_t idesc = instr_desc_bf16(2 * kBM, BN);
+      int g = 0;
+      bool stop = false;
+      int tile, kb, ke;
+      for (int i = 0; !stop && pair_item(sc, K, q, i, tile, kb, ke); ++i) {
+        const int buf = i & 1, use = i >> 1;
+        // the epilogues of both CTAs have read this accumulator's last item
+        if (use > 0 && !mbar_wait(&sh->tmem_empty[buf], (uint32_t)(use - 1) & 1u, abort_flag, status)) {
+          stop = true;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t acc_t = tmem + (uint32_t)buf * acc_cols;
+        for (int kt = kb; kt < ke; ++kt) {
+          const int s = g % stages;
+          const uint32_t ph = (uint32_t)(g / stages) & 1u;
+          if (!mbar_wait(&sh->full[s], ph, abort_flag, status)) {
+            stop = true;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t st = smem_u32(tiles + (size_t)s * stage_bytes);
+          const uint32_t ahi = st, bhi = st + a_bytes;
+          const uint32_t alo = st + a_bytes + b_bytes, blo = st + 2 * a_bytes + b_bytes;
+#pragma unroll
+          for (int kk = 0; kk < kBK / kUmmaK; ++kk) {
+            const uint32_t off = (uint32_t)kk * kUmmaK * 2;
+            const uint32_t acc = (kt > kb || kk > 0) ? 1u : 0u;
+            umma_bf16_pair(acc_t, sw_desc(ahi + off), sw_desc(bhi + off), idesc, acc);
+            if (kSplit) {
+              umma_bf16_pair(acc_t, sw_desc(ahi + off), sw_desc(blo + off), idesc, 1u);
+              umma_bf16_pair(acc_t, sw_desc(alo + off), sw_desc(bhi + off), idesc, 1u);
+            }
+          }
+          umma_commit_pair(&sh->empty[s]);
+          ++g;
+        }
+        if (!stop) umma_commit_pair(&sh->tmem_full[buf]);
+      }
+      if (stop) {
+        umma_commit_pair_local(&sh->drain);
+        mbar_wait_bounded(smem_u32(&sh->drain), 0, nullptr, kMbarWaitNs / 8);
+      }
+    }
+  } else {
+    // epilogue: warps 2..5 -> TMEM lane quarters 2, 3, 0, 1 of this CTA's rows
+    const int quarter = warp & 3;
+    const uint32_t empty_lead0 = map_to_rank(smem_u32(&sh->tmem_empty[0]), 0);
+    const uint32_t empty_lead1 = map_to_rank(smem_u32(&sh->tmem_empty[1]), 0);
+    int tile, kb, ke;
+    for (int i = 0; pair_item(sc, K, q, i, tile, kb, ke); ++i) {
+      const int buf = i & 1, use = i >> 1;
+      const int rt = tile % sc.tiles_m, ct = tile / sc.tiles_m;
+      const int m = rt * (2 * kBM) + (int)rank * kBM + quarter * 32 + lane;
+      const int b0 = ct * BN;
+      const bool with_shift = kb == 0 && shift != 0.f;
+      const bool partial = kb > 0 || ke < K;
+      float sv[16], svn[16];
+      auto load_shift = [&](int c, float(&dst)[16]) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int b = b0 + c + j;
+          dst[j] = (with_shift && m < n && b < p) ? __ldg(Vf + (int64_t)b * ldvf + m) : 0.f;
+        }
+      };
+      load_shift(0, sv);
+      const bool ok =
+          __all_sync(0xffffffffu, mbar_wait<true>(&sh->tmem_full[buf], (uint32_t)use & 1u, abort_flag, status));
+      tc_fence_after();
+      if (!ok) break;
+      const uint32_t acc_t = tmem + (uint32_t)buf * acc_cols + ((uint32_t)(quarter * 32) << 16);
+      for (int c = 0; c < BN; c += 16) {
+        if (c + 16 < BN) load_shift(c + 16, svn);
+        float v[16];
+        tmem_ld16(acc_t + (uint32_t)c, v);
+        if (m < n) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int b = b0 + c + j;
+            if (b < p) {
+              const float out = fmaf(shift, sv[j], v[j]);
+              if (partial)
+                atomicAdd(W + (int64_t)b * ldw + m, out);
+              else
+                W[(int64_t)b * ldw + m] = out;
+            }
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < 16; ++j) sv[j] = svn[j];
+      }
+      // this warp's reads of the accumulator are complete: release it
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0)
+        asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(buf ? empty_lead1 : empty_lead0)
+                     : "memory");
+    }
+  }
+  __syncwarp();
+  tc_fence_before();
+  // neither CTA releases its TMEM or shared memory while the pair's MMAs,
+  // copies, commits or remote arrivals may still reach it
+  cluster_sync_all();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2u * acc_cols)
+                 : "memory");
+  }
+}
+
+// ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
 
@@ -809,8 +1081,9 @@ static int launch_dense_gemv(const __nv_bfloat16 *A_hi, const __nv_bfloat16 *A_l
 // ---------------------------------------------------------------------------
 // Tile configuration rules (set by the autotuner through mfg_gemm_tuning_add):
 // for operators of n in [n_lo, n_hi] applied to p in [p_lo, p_hi] probes, the
-// CTA-pair form uses probe tiles of `bn` columns and splits K in `split`
-// parts (0: the built-in choice).  The last matching rule wins.
+// CTA-pair form uses probe tiles of `bn` columns and `split` selects the
+// form: 1 one tile per pair, 2 K split in two halves, 3 the persistent form
+// (0: the built-in choice).  The last matching rule wins.
 // ---------------------------------------------------------------------------
 struct GemmRule {
   int64_t n_lo, n_hi, p_lo, p_hi;
@@ -823,7 +1096,7 @@ static int g_nrules = 0;
 int gemm_rule_add(int64_t n_lo, int64_t n_hi, int64_t p_lo, int64_t p_hi, int bn, int split) {
   if (n_lo > n_hi || p_lo > p_hi) return MFG_ERR_BAD_ARG;
   if (bn != 0 && (bn < 64 || bn > 256 || bn % 32 != 0)) return MFG_ERR_BAD_ARG;
-  if (split < 0 || split > 2) return MFG_ERR_BAD_ARG;
+  if (split < 0 || split > 3) return MFG_ERR_BAD_ARG;
   std::lock_guard<std::mutex> lk(g_rules_mu);
   if (g_nrules >= 256) return MFG_ERR_SCRATCH_LIMIT;
   g_rules[g_nrules++] = GemmRule{n_lo, n_hi, p_lo, p_hi, bn, split};
@@ -843,6 +1116,42 @@ static GemmRule gemm_rule_for(int64_t n, int64_t p) {
     if (n >= r.n_lo && n <= r.n_hi && p >= r.p_lo && p <= r.p_hi) return r;
   }
   return GemmRule{0, 0, 0, 0, 0, 0};
+}
+
+// Schedule of the persistent form for T tiles of K slices on at most
+// max_pairs CTA pairs (see dense_tcgen05_pair_persistent_kernel); P = 0 when
+// it does not apply.  Tails shorter than min_tail slices are not split off.
+PairSchedule pair_schedule(int64_t T, int tiles_m, int max_pairs, int K, int min_tail) {
+  PairSchedule sc{tiles_m, 0, 0, 0, K};
+  if (T <= 0 || max_pairs < 2 || K <= 0 || T > (1 << 24)) return sc;
+  int P = max_pairs;
+  int F = (int)(T / P), R = (int)(T % P);
+  if (F == 0 && 2 * R <= P) P = 2 * R;  // one main and one tail per tile
+  int Km = K;
+  if (R > 0) {
+    const int c = (R + (P - R) - 1) / (P - R);  // tails of the busiest spare pair
+    Km = (int)(((int64_t)c * K + c) / (c + 1));
+    if (Km > K) Km = K;
+    if (K - Km < min_tail) Km = K;
+  }
+  sc.P = P;
+  sc.F = F;
+  sc.R = R;
+  sc.Km = Km;
+  return sc;
+}
+
+// K slices of the busiest pair
+int64_t schedule_cost(const PairSchedule &sc, int K) {
+  if (sc.P <= 0) return INT64_MAX;
+  int64_t cost = (int64_t)sc.F * K;
+  if (sc.R > 0) {
+    if (sc.Km >= K) return cost + K;
+    const int c = (sc.R + (sc.P - sc.R) - 1) / (sc.P - sc.R);
+    const int64_t tail = (int64_t)c * (K - sc.Km);
+    cost += sc.Km > tail ? sc.Km : tail;
+  }
+  return cost;
 }
 
 int launch_dense_tcgen05(const __nv_bfloat16 *A_hi, const __nv_bfloat16 *A_lo, int64_t lda,
@@ -903,7 +1212,52 @@ int launch_dense_tcgen05(const __nv_bfloat16 *A_hi, const __nv_bfloat16 *A_lo, i
     const int num_k_all = (int)((n + kBK - 1) / kBK);
     const bool split_default = (int64_t)grid.x * grid.y * 5 < (int64_t)sms * 3;
     const bool split_k = rule.split == 0 ? split_default : rule.split == 2;
-    if (split_k && num_k_all >= 4 * stages) {
+    // the persistent form where its schedule is shorter (or a rule asks for it)
+    const int tiles_m = (int)((n + 2 * kBM - 1) / (2 * kBM));
+    const PairSchedule sc = pair_schedule((int64_t)tiles_m * grid.y, tiles_m, sms / 2, num_k_all, stages);
+    if (sc.P > 0 && 2 * (int64_t)sc.P > 2147483647) return MFG_ERR_UNSUPPORTED;
+    const int64_t pairs_t = (int64_t)tiles_m * grid.y;
+    const int64_t waves_plain = (pairs_t + sms / 2 - 1) / (sms / 2);
+    const bool split_ok = split_k && num_k_all >= 4 * stages;
+    const int64_t plain_cost = split_ok ? ((2 * pairs_t + sms / 2 - 1) / (sms / 2)) * ((num_k_all + 1) / 2)
+                                        : waves_plain * num_k_all;
+    // Filling the idle SMs also lowers the clock under the power cap (n =
+    // 16384, 256 probes: 1.76 -> 1.67 GHz, no net gain), so by default only
+    // schedules at least 15 % shorter take the persistent form.
+    const bool persistent = sc.P > 0 && (rule.split == 3 ||
+                                         (rule.split == 0 && schedule_cost(sc, num_k_all) * 100 <= plain_cost * 85));
+    if (persistent) {
+      if (sc.R > 0 && sc.Km < num_k_all) {
+        // the split (remainder) tiles add two partial products into zeroed W
+        if (grid.y == 1) {
+          const int64_t r0 = (int64_t)sc.F * sc.P * 2 * kBM;
+          MFG_CUDA_TRY(cudaMemset2DAsync(W + r0, (size_t)ldw * sizeof(float), 0,
+                                         (size_t)(n - r0) * sizeof(float), (size_t)p, s));
+        } else {
+          MFG_CUDA_TRY(cudaMemset2DAsync(W, (size_t)ldw * sizeof(float), 0, (size_t)n * sizeof(float),
+                                         (size_t)p, s));
+        }
+      }
+      uint32_t acc_cols = 32;
+      while ((int)acc_cols < BN) acc_cols <<= 1;
+      const size_t smem_p = 1024 + (size_t)stages * stage_bytes + sizeof(GemmSharedP);
+      dim3 pgrid((unsigned)(2 * sc.P), 1, 1);
+      if (split) {
+        MFG_CUDA_TRY(cudaFuncSetAttribute(dense_tcgen05_pair_persistent_kernel<true>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_p));
+        dense_tcgen05_pair_persistent_kernel<true><<<pgrid, kGemmThreads, smem_p, s>>>(
+            mahi, malo, mbhi, mblo, Vf, ldvf, W, ldw, (int)n, (int)p, BN, stages, acc_cols, sc,
+            (float)shift, status);
+      } else {
+        MFG_CUDA_TRY(cudaFuncSetAttribute(dense_tcgen05_pair_persistent_kernel<false>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_p));
+        dense_tcgen05_pair_persistent_kernel<false><<<pgrid, kGemmThreads, smem_p, s>>>(
+            mahi, malo, mbhi, mblo, Vf, ldvf, W, ldw, (int)n, (int)p, BN, stages, acc_cols, sc,
+            (float)shift, status);
+      }
+      return MFG_LAUNCH_STATUS();
+    }
+    if (split_ok) {
       grid.z = 2;
       MFG_CUDA_TRY(cudaMemset2DAsync(W, (size_t)ldw * sizeof(float), 0, (size_t)n * sizeof(float),
                                      (size_t)p, s));
@@ -942,3 +1296,34 @@ int launch_dense_tcgen05(const __nv_bfloat16 *A_hi, const __nv_bfloat16 *A_lo, i
 }
 
 }  // namespace mfg
+
+extern "C" {
+
+// Work list of the persistent CTA-pair form (host only; see the header).
+MFG_API int64_t mfg_gemm_pair_schedule(int64_t n, int64_t p, int32_t bn, int32_t max_pairs,
+                                       int32_t min_tail, int32_t *items, int64_t capacity) {
+  using namespace mfg;
+  if (n <= 0 || p <= 0 || bn < 16 || bn > 256 || bn % 16 != 0 || max_pairs < 2 || min_tail < 0)
+    return -(int64_t)MFG_ERR_BAD_ARG;
+  if (n >= (1ll << 31) || p >= (1ll << 31)) return -(int64_t)MFG_ERR_BAD_ARG;
+  const int K = (int)((n + kBK - 1) / kBK);
+  const int tiles_m = (int)((n + 2 * kBM - 1) / (2 * kBM));
+  const int64_t T = (int64_t)tiles_m * ((p + bn - 1) / bn);
+  const PairSchedule sc = pair_schedule(T, tiles_m, max_pairs, K, min_tail);
+  if (sc.P <= 0) return -(int64_t)MFG_ERR_UNSUPPORTED;
+  int64_t count = 0;
+  for (int q = 0; q < sc.P; ++q) {
+    int tile, kb, ke;
+    for (int i = 0; pair_item(sc, K, q, i, tile, kb, ke); ++i, ++count) {
+      if (items && count < capacity) {
+        items[4 * count] = q;
+        items[4 * count + 1] = tile;
+        items[4 * count + 2] = kb;
+        items[4 * count + 3] = ke;
+      }
+    }
+  }
+  return count;
+}
+
+}  // extern "C"

@@ -131,4 +131,7 @@ int launch_dense_tcgen05(const __nv_bfloat16 *A_hi, const __nv_bfloat16 *A_lo, i
                          int64_t p, double shift, int *status, cudaStream_t s);
 bool tcgen05_supported_shape(int64_t n, int64_t p);
 
+// wait_selftest.cu: a bounded wait on an mbarrier nothing arrives on
+int launch_wait_selftest(uint64_t limit_ns, int *status, unsigned long long *times, cudaStream_t s);
+
 }  // namespace mfg

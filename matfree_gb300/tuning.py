@@ -4,8 +4,10 @@ The CTA-pair GEMM covers an n x n operator with ceil(n / 256) row tiles per
 probe tile.  With 76 CTA pairs on the GPU, some sizes fill the SMs in whole
 waves and others leave up to half of them idle in a last partial wave
 (n = 20000: 79 tiles, 1.04 waves).  Narrower probe tiles (more tiles, the
-operator re-read once per tile) or a K split over two CTAs (partial products
-added into W) change the wave count.  Which of these is fastest depends on n,
+operator re-read once per tile), a K split over two CTAs (partial products
+added into W) or the persistent form (one pair per two SMs; the last wave's
+tiles split once along K, their tails packed onto the spare pairs) change
+the wave count.  Which of these is fastest depends on n,
 p and the precision, so ``autotune`` times every candidate on the device for a
 grid of operator sizes and probe counts and installs the winners as rules in
 the library (``mfg_gemm_tuning_add``); ``save`` / ``load`` keep them in a
@@ -24,7 +26,9 @@ import torch
 from . import _lib
 from ._panel import Workspace, padded_ld, stream_ptr
 
-CANDIDATES = ((0, 0), (0, 2), (128, 1), (128, 2), (64, 1))  # (probe tile, K split); 0: built-in
+# (probe tile, form): 0 built-in; form 1 one tile per CTA pair, 2 K halves,
+# 3 persistent pairs with the last wave split along K
+CANDIDATES = ((0, 0), (0, 1), (0, 2), (0, 3), (128, 1), (128, 2), (128, 3), (64, 1))
 DEFAULT_NS = tuple(int(round(1024 * 2 ** (i / 2))) // 8 * 8 for i in range(11))  # 1024 .. 32768
 DEFAULT_PS = (32, 64, 128, 256)
 
@@ -140,3 +144,62 @@ def ensure(precision="bf16x3", **kwargs):
         rules = autotune(precision=precision, **kwargs)
         save(rules, precision=precision)
     return rules
+
+
+def time_form(n: int, p: int, bn: int = 0, form: int = 0, precision: str = "bf16x3", reps: int = 10,
+              seed: int = 0, device="cuda") -> dict:
+    """Median device time of one operator product (n x n, p probes) under the
+    tile rule (bn, form); L2 flushed before each timed launch."""
+    from .operators import DenseOperator
+
+    lib = _lib.lib()
+    ld = padded_ld(n)
+    g = torch.Generator(device=device).manual_seed(seed)
+    A = torch.randn((n, n), device=device, generator=g) / math.sqrt(n)
+    op = DenseOperator(A, precision=precision, shift=0.01)
+    del A
+    s = op.c_struct()
+    panel = torch.zeros((p, ld), dtype=torch.float32, device=device)
+    panel[:, :n].normal_(generator=g)
+    out = torch.zeros_like(panel)
+    ws = Workspace()
+    ws.get(lib.mfg_slq_workspace_bytes(ctypes.byref(s), 0, p, ld), device)
+    flush = torch.empty(64 << 20, dtype=torch.float32, device=device)  # 256 MB > L2
+    lib.mfg_gemm_tuning_clear()
+    try:
+        if bn or form:
+            _lib.check(lib.mfg_gemm_tuning_add(n, n, p, p, bn, form), "mfg_gemm_tuning_add")
+        args = (ctypes.byref(s), ctypes.c_void_p(panel.data_ptr()), ctypes.c_void_p(out.data_ptr()),
+                p, ld, ctypes.c_void_p(ws.buf.data_ptr()), ws.buf.numel(), stream_ptr())
+        for _ in range(2):
+            _lib.check(lib.mfg_operator_apply(*args), "mfg_operator_apply")
+        times = []
+        for _ in range(reps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            _lib.check(lib.mfg_operator_apply(*args), "mfg_operator_apply")
+            e1.record()
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1))
+    finally:
+        lib.mfg_gemm_tuning_clear()
+    times.sort()
+    ms = times[len(times) // 2]
+    flop = (3 if precision == "bf16x3" else 1) * 2.0 * n * n * p
+    return {"n": n, "p": p, "bn": bn, "form": form, "precision": precision, "median_ms": ms,
+            "tflops": flop / (ms * 1e-3) / 1e12}
+
+
+if __name__ == "__main__":
+    import argparse
+
+    ap = argparse.ArgumentParser(description="time one tensor-core operator product under a tile rule")
+    ap.add_argument("--n", type=int, default=16384)
+    ap.add_argument("--p", type=int, default=256)
+    ap.add_argument("--bn", type=int, default=0)
+    ap.add_argument("--form", type=int, default=0, help="0 built-in, 1 one tile per pair, 2 K halves, 3 persistent")
+    ap.add_argument("--precision", default="bf16x3")
+    ap.add_argument("--reps", type=int, default=10)
+    a = ap.parse_args()
+    print(json.dumps(time_form(a.n, a.p, a.bn, a.form, a.precision, a.reps)))

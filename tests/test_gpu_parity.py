@@ -443,3 +443,47 @@ def test_autotuner_installs_rules_that_keep_the_product():
         assert np.abs(W.double().cpu().numpy() - want).max() / np.abs(want).max() < 5e-5
     finally:
         _lib.lib().mfg_gemm_tuning_clear()
+
+
+@pytest.mark.parametrize("precision", ["bf16x3", "bf16"])
+@pytest.mark.parametrize("n,p", [(4608, 256),    # 18 tiles: each split in two halves on 36 pairs
+                                 (16384, 256),   # 64 tiles on 76 pairs: 6 tails per spare pair
+                                 (20000, 64),    # a full wave of 76 tiles, 3 split remainder tiles
+                                 (5000, 700),    # three probe tiles (256, 256, 188)
+                                 (3000, 96)])
+def test_persistent_pair_form_matches_float64_and_is_deterministic(precision, n, p):
+    from matfree_gb300 import _lib
+
+    rng = np.random.default_rng(n + p)
+    A = rng.standard_normal((n, n)) / np.sqrt(n)
+    V = rng.standard_normal((p, n))
+    lib = _lib.lib()
+    try:
+        assert lib.mfg_gemm_tuning_add(n, n, p, p, 0, 3) == 0
+        op = mf.DenseOperator(_t(A, torch.float32), precision=precision, shift=0.5)
+        Vt = _t(V, torch.float32)
+        W1 = op.matmat(Vt)
+        W2 = op.matmat(Vt)
+        lib.mfg_gemm_tuning_clear()
+        assert lib.mfg_gemm_tuning_add(n, n, p, p, 0, 1) == 0
+        W0 = op.matmat(Vt)
+    finally:
+        lib.mfg_gemm_tuning_clear()
+    # two partial products per split tile: the sum does not depend on timing
+    assert torch.equal(W1, W2)
+    if precision == "bf16":
+        A_s = op.dense().double().cpu().numpy() - 0.5 * np.eye(n)
+        V_s = V.astype(np.float32).astype(np.float64)
+        V_b = torch.tensor(V_s).to(torch.bfloat16).double().numpy()
+        want = V_b @ A_s.T + 0.5 * V_s
+    else:
+        A32 = A.astype(np.float32).astype(np.float64)
+        V32 = V.astype(np.float32).astype(np.float64)
+        want = V32 @ A32.T + 0.5 * V32
+    tol = 5e-5  # the tensor pipe's truncating fp32 accumulation, as in the apply tests
+    W = W1.double().cpu().numpy()
+    err = np.abs(W - want).max() / np.abs(want).max()
+    assert err < tol * max(1.0, n / 8192), err
+    # against one tile per pair: the same product up to the K split's rounding
+    d = (W1.double() - W0.double()).abs().max().item() / np.abs(want).max()
+    assert d < 2 * tol * max(1.0, n / 8192), d

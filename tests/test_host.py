@@ -246,7 +246,8 @@ def test_tuning_rule_ranges_tile_the_axis():
 def test_gemm_tuning_rejects_bad_rules():
     lib = _lib.lib()
     assert lib.mfg_gemm_tuning_add(1024, 2048, 64, 64, 48, 0) == _lib.MFG_ERR_BAD_ARG  # not a multiple of 32
-    assert lib.mfg_gemm_tuning_add(1024, 2048, 64, 64, 128, 3) == _lib.MFG_ERR_BAD_ARG
+    assert lib.mfg_gemm_tuning_add(1024, 2048, 64, 64, 128, 4) == _lib.MFG_ERR_BAD_ARG
+    assert lib.mfg_gemm_tuning_add(1024, 2048, 64, 64, 128, 3) == _lib.MFG_OK
     assert lib.mfg_gemm_tuning_add(2048, 1024, 64, 64, 128, 1) == _lib.MFG_ERR_BAD_ARG
     assert lib.mfg_gemm_tuning_add(1024, 2048, 64, 64, 128, 1) == _lib.MFG_OK
     assert lib.mfg_gemm_tuning_clear() == _lib.MFG_OK
