@@ -1545,40 +1545,91 @@ int launch_sub2(const T *Q, int64_t q_bstride, int64_t q_istride, int coff, int 
   return launch_stream_sweep<T, kStreamSub2>(a, s);
 }
 
-// One warp per probe: the coefficient algebra of step j >= 1 (see above).
+// One CTA of four warps per probe: the coefficient algebra of step j >= 1
+// (see above).
 // X2: [Q^T qt (j) | Q^T w (j) at koff | qt . w at 2 koff], dots: (||b'||^2,
 // ||z||^2, b' . z) with b' = qt - Q Q^T qt, z = w - Q Q^T w.  Writes H row/col
 // entries of the reference's H, the full coefficients Hh ((k + 1) x k), the
 // next scale nu and the finish coefficients cf = (1/rho, 1/s, qw/(rho s)).
 // Hh is stored column-major ((k + 1) rows a column) so that a column update
 // and the product Hh h2 read and write consecutive words across the lanes.
-__global__ void twosweep_coef_kernel(int j, int k, int64_t p, const double *__restrict__ X2,
-                                     int64_t koff, const double *__restrict__ dots,
-                                     double *__restrict__ H, double *__restrict__ Hh,
-                                     double *__restrict__ nu, double *__restrict__ cf,
-                                     int *__restrict__ status) {
+// The product's stored columns 0 .. j - 2 are cut into four contiguous
+// ranges, one per warp (a quarter of the dependent load rounds); warp 0 adds
+// the four partial sums in warp order and finishes alone.
+constexpr int kCoefWarps = 4;
+
+__global__ void __launch_bounds__(32 * kCoefWarps)
+twosweep_coef_kernel(int j, int k, int64_t p, const double *__restrict__ X2, int64_t koff,
+                     const double *__restrict__ dots, double *__restrict__ H,
+                     double *__restrict__ Hh, double *__restrict__ nu, double *__restrict__ cf,
+                     int *__restrict__ status) {
   // j <= kTwoSweepMaxK - 1 = 128: columns in 4 blocks of 32 lanes, rows
   // (0 .. j) in 5 blocks
   constexpr int kCB = 4, kRB = 5;
-  const int lane = threadIdx.x & 31;
-  const int64_t b = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (b >= p) return;  // warp-uniform
+  __shared__ double msum[kCoefWarps][kRB * 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t b = blockIdx.x;
+  if (b >= p) return;  // block-uniform
   const double *x = X2 + b * (2 * koff + 1);
   double *Hb = H + b * (int64_t)k * k;
   double *Hhb = Hh + b * (int64_t)(k + 1) * k;  // column-major: column l at Hhb + l (k + 1)
   const int64_t ld = k + 1;
-  // every input first, in one round of independent loads
-  const double nb = dots[b * 3], nz = dots[b * 3 + 1], bz = dots[b * 3 + 2];
-  const double c = x[2 * koff], nuj = nu[b];
+  // warp 0: every input of the finishing algebra first, in one round of
+  // independent loads; all warps: Q^T qt (the product's vector)
+  double nb = 0.0, nz = 0.0, bz = 0.0, c = 0.0, nuj = 0.0;
   double hq[kCB], g[kCB], hp[kCB];
+  if (warp == 0) {
+    nb = dots[b * 3];
+    nz = dots[b * 3 + 1];
+    bz = dots[b * 3 + 2];
+    c = x[2 * koff];
+    nuj = nu[b];
+  }
 #pragma unroll
   for (int cb = 0; cb < kCB; ++cb) {
     const int l = lane + 32 * cb;
     const bool ok = l < j;
     hq[cb] = ok ? x[l] : 0.0;
-    g[cb] = ok ? x[koff + l] : 0.0;
-    hp[cb] = ok ? Hb[(int64_t)l * k + (j - 1)] : 0.0;
+    g[cb] = (ok && warp == 0) ? x[koff + l] : 0.0;
+    hp[cb] = (ok && warp == 0) ? Hb[(int64_t)l * k + (j - 1)] : 0.0;
   }
+  if (j < k) {
+    // partial m = Hh[0:j+1, cols] hq over this warp's columns: all lanes walk
+    // the same columns (hq_l broadcast by shuffle), eight columns of loads
+    // in flight; entries below the subdiagonal (never written) are masked
+    const int ncol = j - 1;
+    const int per = (ncol + kCoefWarps - 1) / kCoefWarps;
+    const int lb = warp * per;
+    const int le = lb + per < ncol ? lb + per : ncol;
+    double m[kRB];
+#pragma unroll
+    for (int r = 0; r < kRB; ++r) m[r] = 0.0;
+    for (int l0 = lb; l0 < le; l0 += 8) {
+      double a[8][kRB];
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        const int l = l0 + t;
+        const double *cl = Hhb + (int64_t)l * ld;
+#pragma unroll
+        for (int r = 0; r < kRB; ++r) {
+          const int i = lane + 32 * r;
+          a[t][r] = (l < le && i <= l + 1) ? cl[i] : 0.0;
+        }
+      }
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        const int l = l0 + t;
+        const double src = l < 32 ? hq[0] : (l < 64 ? hq[1] : (l < 96 ? hq[2] : hq[3]));
+        const double hv = __shfl_sync(0xffffffffu, src, l & 31);
+#pragma unroll
+        for (int r = 0; r < kRB; ++r) m[r] = fma(a[t][r], hv, m[r]);
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < kRB; ++r) msum[warp][r * 32 + lane] = m[r];
+  }
+  __syncthreads();
+  if (warp != 0) return;
   double hh = 0.0, hg = 0.0;
 #pragma unroll
   for (int cb = 0; cb < kCB; ++cb) {
@@ -1605,32 +1656,12 @@ __global__ void twosweep_coef_kernel(int j, int k, int64_t p, const double *__re
   if (lane == 0) Hb[(int64_t)j * k + (j - 1)] = beta;
   const double qw = (c - hg) / rho;  // q_j . A qt_j
   if (j < k) {
-    // m = Hh[0:j+1, 0:j] hq: all lanes walk the same columns (hq_l broadcast
-    // by shuffle), eight columns of loads in flight; entries below the
-    // subdiagonal (never written) are masked
     double m[kRB];
 #pragma unroll
-    for (int r = 0; r < kRB; ++r) m[r] = 0.0;
-    for (int l0 = 0; l0 < j - 1; l0 += 8) {
-      double a[8][kRB];
+    for (int r = 0; r < kRB; ++r) {
+      m[r] = msum[0][r * 32 + lane];
 #pragma unroll
-      for (int t = 0; t < 8; ++t) {
-        const int l = l0 + t;
-        const double *cl = Hhb + (int64_t)l * ld;
-#pragma unroll
-        for (int r = 0; r < kRB; ++r) {
-          const int i = lane + 32 * r;
-          a[t][r] = (l < j - 1 && i <= l + 1) ? cl[i] : 0.0;
-        }
-      }
-#pragma unroll
-      for (int t = 0; t < 8; ++t) {
-        const int l = l0 + t;
-        const double src = l < 32 ? hq[0] : (l < 64 ? hq[1] : (l < 96 ? hq[2] : hq[3]));
-        const double hv = __shfl_sync(0xffffffffu, src, l & 31);
-#pragma unroll
-        for (int r = 0; r < kRB; ++r) m[r] = fma(a[t][r], hv, m[r]);
-      }
+      for (int w = 1; w < kCoefWarps; ++w) m[r] += msum[w][r * 32 + lane];
     }
     {
       const int l = j - 1;
@@ -1722,8 +1753,9 @@ int launch_twosweep_coef(int j, int k, int64_t p, const double *X2, int64_t koff
                          const double *dots, double *H, double *Hh, double *nu, double *cf,
                          int *status, cudaStream_t s) {
   if (p <= 0) return MFG_OK;
-  twosweep_coef_kernel<<<(unsigned)ceil_div(p, 4), 128, 0, s>>>(j, k, p, X2, koff, dots, H, Hh,
-                                                                nu, cf, status);
+  if (p > 2147483647) return MFG_ERR_UNSUPPORTED;
+  twosweep_coef_kernel<<<(unsigned)p, 32 * kCoefWarps, 0, s>>>(j, k, p, X2, koff, dots, H, Hh, nu,
+                                                               cf, status);
   return MFG_LAUNCH_STATUS();
 }
 

@@ -531,15 +531,27 @@ rbf8_kernel(const float *__restrict__ x, int64_t n, int dim, float s2, float inv
   __syncthreads();
   const int64_t j0 = c0 + (int64_t)threadIdx.x * 8;
   if (j0 >= lda) return;
+  // this thread's 8 points in registers, read from shared memory once (a
+  // read per row would be an 8-way bank conflict: threads are 8 floats
+  // apart); dimensions past dim are zero on both sides and add nothing
+  float xc[kRbfMaxDim][8];
+#pragma unroll
+  for (int d = 0; d < kRbfMaxDim; ++d)
+#pragma unroll
+    for (int e = 0; e < 8; ++e) xc[d][e] = d < dim ? xs[d][threadIdx.x * 8 + e] : 0.f;
   for (int rr = 0; rr < kRbfRows; ++rr) {
     const int64_t i = r0 + rr;
     if (i >= n) return;
+    float xi[kRbfMaxDim];
+#pragma unroll
+    for (int d = 0; d < kRbfMaxDim; ++d) xi[d] = d < dim ? __ldg(x + i * dim + d) : 0.f;
     float v[8];
 #pragma unroll
     for (int e = 0; e < 8; ++e) {
       float d2 = 0.f;
-      for (int d = 0; d < dim; ++d) {
-        const float df = x[i * dim + d] - xs[d][threadIdx.x * 8 + e];
+#pragma unroll
+      for (int d = 0; d < kRbfMaxDim; ++d) {
+        const float df = xi[d] - xc[d][e];
         d2 = fmaf(df, df, d2);
       }
       float w = s2 * expf(-d2 * inv2l2);
