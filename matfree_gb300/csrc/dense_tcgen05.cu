@@ -546,7 +546,9 @@ dense_tcgen05_pair_kernel(const __grid_constant__ CUtensorMap map_ahi,
 //     tile F P + q (q < R), or the tail K range [Km, K) of the remainder
 //     tiles e, e + (P - R), e + 2 (P - R), ... (e = q - R).
 // Km balances the main piece against the c = ceil(R / (P - R)) tails of the
-// busiest spare pair.  A split tile thus has exactly two partial products,
+// busiest spare pair.  Tiles are split only when there are no full waves
+// (F = 0), so every output row has the same accumulation structure.  A split
+// tile has exactly two partial products,
 // which add into a zeroed W: a two-term sum is the same in either order, so
 // the result does not depend on timing.  The piece that starts at K = 0
 // adds the shift term.
@@ -1128,7 +1130,13 @@ PairSchedule pair_schedule(int64_t T, int tiles_m, int max_pairs, int K, int min
   int F = (int)(T / P), R = (int)(T % P);
   if (F == 0 && 2 * R <= P) P = 2 * R;  // one main and one tail per tile
   int Km = K;
-  if (R > 0) {
+  // Split only when every tile is split at the same K slice (no full
+  // waves): the tensor pipe's fp32 accumulation truncates, so an output's
+  // rounding bias depends on the length of its accumulation chains, and
+  // rows with a K split next to rows without one turn a symmetric operator
+  // into a slightly non-symmetric one (n = 29368, 64 probes: 5e-5 between
+  // the two kinds of rows, a 3e-4 log-determinant error under Lanczos).
+  if (R > 0 && F == 0) {
     const int c = (R + (P - R) - 1) / (P - R);  // tails of the busiest spare pair
     Km = (int)(((int64_t)c * K + c) / (c + 1));
     if (Km > K) Km = K;

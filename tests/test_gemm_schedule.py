@@ -10,6 +10,9 @@ kernel's correctness rests on:
   K slice 0 (it adds the shift term), so the two partial products add into a
   zeroed output in an order that cannot change the sum;
 * every item lies inside the grid (pair < P, tile < T, 0 <= kb < ke <= K);
+* if any tile is split, every tile is split at the same K slice: the tensor
+  pipe's accumulation rounding depends on the chain length, and a mix of
+  split and unsplit rows would make a symmetric operator non-symmetric;
 * the busiest pair's K slices match the schedule's cost (n = 16384, 256
   probes on 76 pairs: 439 of 512).
 """
@@ -52,6 +55,9 @@ def _check(n, p, bn, pairs, min_tail):
         if len(ps) == 2:
             assert ps[0][1] == ps[1][0], (t, ps)
             assert ps[1][1] - ps[1][0] >= min_tail
+    splits = {ps[0][1] for ps in pieces.values() if len(ps) == 2}
+    if splits:
+        assert len(splits) == 1 and all(len(ps) == 2 for ps in pieces.values()), splits
     load = defaultdict(int)
     for q, _, kb, ke in items:
         load[int(q)] += int(ke - kb)

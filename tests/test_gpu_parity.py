@@ -448,7 +448,7 @@ def test_autotuner_installs_rules_that_keep_the_product():
 @pytest.mark.parametrize("precision", ["bf16x3", "bf16"])
 @pytest.mark.parametrize("n,p", [(4608, 256),    # 18 tiles: each split in two halves on 36 pairs
                                  (16384, 256),   # 64 tiles on 76 pairs: 6 tails per spare pair
-                                 (20000, 64),    # a full wave of 76 tiles, 3 split remainder tiles
+                                 (20000, 64),    # 79 tiles: a full wave, the rest unsplit (no mixed rows)
                                  (5000, 700),    # three probe tiles (256, 256, 188)
                                  (3000, 96)])
 def test_persistent_pair_form_matches_float64_and_is_deterministic(precision, n, p):
