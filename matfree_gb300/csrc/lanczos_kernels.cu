@@ -533,7 +533,11 @@ __host__ __device__ constexpr int stream_nout_max() {
                                : (kMode == kStreamSub2 ? 3 : (kMode == kStreamSubNorm ? 1 : kSPGroup * MAXG));
 }
 
-template <typename T, int MAXG, bool kHold, int kMode>
+// kRPT: rows of a chunk per row thread (chunks of kSR * kRPT rows).  Chunks
+// of few vectors are small, and a pass over them is bound by the number of
+// bulk copies and per-chunk steps rather than by bytes; the two-sweep modes
+// with at most 8 vectors take 4 rows a thread (2 KB copies, 1-D only).
+template <typename T, int MAXG, bool kHold, int kMode, int kRPT = 1>
 __global__ void __launch_bounds__(kSThreads + 32)
 stream_sweep_kernel(const __grid_constant__ CUtensorMap qmap, const T *__restrict__ Q,
                     int64_t q_bstride, int64_t q_istride, int ncols,
@@ -549,15 +553,17 @@ stream_sweep_kernel(const __grid_constant__ CUtensorMap qmap, const T *__restric
   constexpr bool kDots = kMode == kStreamSubProj || kMode == kStreamProj || kMode == kStreamProj2;
   constexpr int kNV = kPair ? 2 : 1;
   constexpr int kNAcc = kDots ? kSPGroup * MAXG : 1;
+  static_assert(kRPT == 1 || !kHold, "register-held basis values are for one row a thread");
+  constexpr int CR = kSR * kRPT;  // rows of a chunk
   extern __shared__ __align__(128) uint8_t smem[];
   const int ngroups = (ncols + kSPGroup - 1) / kSPGroup;
   const int cpad = ngroups * kSPGroup;
   const int nout = kMode == kStreamProj2 || kMode == kStreamSub2 ? stream_nout_max<MAXG, kMode>()
                                                                  : (kDots ? ncols : 1);
-  // ring of nbuf buffers [cpad + kNV][kSR]: the chunk's basis rows (zero
+  // ring of nbuf buffers [cpad + kNV][CR]: the chunk's basis rows (zero
   // columns past ncols), then its rows of w (and of the second vector)
   T *bufs = reinterpret_cast<T *>(smem);
-  const size_t bstr = (size_t)(cpad + kNV) * kSR;
+  const size_t bstr = (size_t)(cpad + kNV) * CR;
   T *s_coef = bufs + nbuf * bstr;  // [kNV][cpad], zero past ncols
   __shared__ __align__(8) uint64_t full_bar[kSMaxBuf];   // copies of the chunk landed
   __shared__ __align__(8) uint64_t empty_bar[kSMaxBuf];  // every row warp is done with it
@@ -566,7 +572,7 @@ stream_sweep_kernel(const __grid_constant__ CUtensorMap qmap, const T *__restric
   __shared__ int s_last;
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int64_t C = (n + kSR - 1) / kSR;
+  const int64_t C = (n + CR - 1) / CR;
   const int64_t F = p * C;
   const int64_t G = gridDim.x;
   const int64_t f_begin = F * (int64_t)blockIdx.x / G;
@@ -585,12 +591,15 @@ stream_sweep_kernel(const __grid_constant__ CUtensorMap qmap, const T *__restric
   }
   if (threadIdx.x < kSR)
     for (int u = 0; u < nbuf; ++u)
-      for (int i = ncols; i < cpad; ++i) bufs[u * bstr + (size_t)i * kSR + threadIdx.x] = (T)0;
+      for (int i = ncols; i < cpad; ++i)
+#pragma unroll
+        for (int rr = 0; rr < kRPT; ++rr) bufs[u * bstr + (size_t)i * CR + rr * kSR + threadIdx.x] = (T)0;
   // 2-D tensor copies need a 128-byte aligned shared destination; if the
   // ring is not aligned, record it and load every vector with 1-D copies
   const bool tile_ok = (smem_addr(bufs) & 127u) == 0;
   if (!tile_ok && threadIdx.x == 0 && status) atomicExch(status, (int)MFG_ERR_BAD_ARG);
-  const int full = tile_ok ? ncols / kSPGroup : 0;
+  // (2-D boxes are kSR rows high: chunks of several rows a thread use 1-D copies)
+  const int full = (tile_ok && kRPT == 1) ? ncols / kSPGroup : 0;
   __syncthreads();
   volatile int *fail = &s_fail;
 
@@ -614,8 +623,8 @@ stream_sweep_kernel(const __grid_constant__ CUtensorMap qmap, const T *__restric
         }
         break;
       }
-      const int64_t r0 = c * kSR;
-      const int64_t rows = (n - r0 < kSR) ? (n - r0) : kSR;
+      const int64_t r0 = c * CR;
+      const int64_t rows = (n - r0 < CR) ? (n - r0) : CR;
       const uint32_t seg_bytes = (uint32_t)(((rows * (int64_t)sizeof(T)) + 15) / 16 * 16);
       const uint32_t bytes = (uint32_t)full * (uint32_t)(kSPGroup * kSR * sizeof(T)) +
                              seg_bytes * (uint32_t)(ncols - full * kSPGroup + kNV);
@@ -642,7 +651,7 @@ stream_sweep_kernel(const __grid_constant__ CUtensorMap qmap, const T *__restric
           const T *src = vec == 0   ? Wv + b * w_bstride + r0
                          : vec == 1 ? Wv2 + b * w2_bstride + r0
                                     : Q + b * q_bstride + (int64_t)(coff + i) * q_istride + r0;
-          T *d = dst + (size_t)(vec >= 0 ? cpad + vec : i) * kSR;
+          T *d = dst + (size_t)(vec >= 0 ? cpad + vec : i) * CR;
           asm volatile(
               "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
               ::"r"(smem_addr(d)), "l"(reinterpret_cast<uint64_t>(src)), "r"(seg_bytes),
@@ -706,93 +715,97 @@ stream_sweep_kernel(const __grid_constant__ CUtensorMap qmap, const T *__restric
           if (status) atomicExch(status, (int)MFG_ERR_TIMEOUT);
         }
       }
-      const T *buf = bufs + u * bstr + j;  // this thread's row, column stride kSR
-      const int64_t r0 = c * kSR;
-      const int rows = (int)((n - r0 < kSR) ? (n - r0) : kSR);
-      T qv[kHold ? kSPGroup * MAXG : 1];
-      T w = ready ? buf[(size_t)cpad * kSR] : (T)0;
-      T w2v = (kPair && ready) ? buf[(size_t)(cpad + 1) * kSR] : (T)0;  // second vector
-      if constexpr (kMode == kStreamSub2) {
-        // b' = b - Q h and a' = a - Q g over this thread's row
-        T a0 = w, a1 = (T)0, b0 = w2v, b1 = (T)0;
+      const int64_t r0 = c * CR;
+      const int rows = (int)((n - r0 < CR) ? (n - r0) : CR);
 #pragma unroll
-        for (int g = 0; g < MAXG; ++g)
-          if (ready && g < ngroups) {
-#pragma unroll
-            for (int e = 0; e < kSPGroup; e += 2) {
-              const int i = g * kSPGroup + e;
-              const T q0 = buf[(size_t)i * kSR], q1 = buf[(size_t)(i + 1) * kSR];
-              b0 = fma(-q0, s_coef[i], b0);
-              b1 = fma(-q1, s_coef[i + 1], b1);
-              a0 = fma(-q0, s_coef[cpad + i], a0);
-              a1 = fma(-q1, s_coef[cpad + i + 1], a1);
-            }
-          }
-        w = a0 + a1;
-        w2v = b0 + b1;
-      } else if constexpr (kUpdate) {
-        // w' = w - Q c over this thread's row; four interleaved sums shorten
-        // the dependent chain
-        T w0 = w, w1 = (T)0, w2 = (T)0, w3 = (T)0;
-#pragma unroll
-        for (int g = 0; g < MAXG; ++g)
-          if (ready && g < ngroups) {
-#pragma unroll
-            for (int e = 0; e < kSPGroup; e += 4) {
-              const int i = g * kSPGroup + e;
-              const T q0 = buf[(size_t)i * kSR], q1 = buf[(size_t)(i + 1) * kSR];
-              const T q2 = buf[(size_t)(i + 2) * kSR], q3 = buf[(size_t)(i + 3) * kSR];
-              if constexpr (kHold) {
-                qv[i] = q0;
-                qv[i + 1] = q1;
-                qv[i + 2] = q2;
-                qv[i + 3] = q3;
-              }
-              w0 = fma(-q0, s_coef[i], w0);
-              w1 = fma(-q1, s_coef[i + 1], w1);
-              w2 = fma(-q2, s_coef[i + 2], w2);
-              w3 = fma(-q3, s_coef[i + 3], w3);
-            }
-          }
-        w = (w0 + w1) + (w2 + w3);
-      }
-      // rows past the probe's end hold stale shared memory and are left out
-      if (ready && j < rows) {
-        if constexpr (kUpdate) Wv[b * w_bstride + r0 + j] = w;
-        if constexpr (kMode == kStreamSubNorm) {
-          const T w2 = w * w;
-          nrm += (double)w2;
-        }
+      for (int rr = 0; rr < kRPT; ++rr) {
+        const int jr = j + rr * kSR;            // this thread's row of the chunk
+        const T *buf = bufs + u * bstr + jr;  // column stride CR
+        T qv[kHold ? kSPGroup * MAXG : 1];
+        T w = ready ? buf[(size_t)cpad * CR] : (T)0;
+        T w2v = (kPair && ready) ? buf[(size_t)(cpad + 1) * CR] : (T)0;  // second vector
         if constexpr (kMode == kStreamSub2) {
-          Wo2[b * wo2_bstride + r0 + j] = w2v;
-          nrm += (double)(w2v * w2v);
-          nrm2 += (double)(w * w);
-          dot2 += (double)(w2v * w);
+          // b' = b - Q h and a' = a - Q g over this thread's row
+          T a0 = w, a1 = (T)0, b0 = w2v, b1 = (T)0;
+#pragma unroll
+          for (int g = 0; g < MAXG; ++g)
+            if (ready && g < ngroups) {
+#pragma unroll
+              for (int e = 0; e < kSPGroup; e += 2) {
+                const int i = g * kSPGroup + e;
+                const T q0 = buf[(size_t)i * CR], q1 = buf[(size_t)(i + 1) * CR];
+                b0 = fma(-q0, s_coef[i], b0);
+                b1 = fma(-q1, s_coef[i + 1], b1);
+                a0 = fma(-q0, s_coef[cpad + i], a0);
+                a1 = fma(-q1, s_coef[cpad + i + 1], a1);
+              }
+            }
+          w = a0 + a1;
+          w2v = b0 + b1;
+        } else if constexpr (kUpdate) {
+          // w' = w - Q c over this thread's row; four interleaved sums shorten
+          // the dependent chain
+          T w0 = w, w1 = (T)0, w2 = (T)0, w3 = (T)0;
+#pragma unroll
+          for (int g = 0; g < MAXG; ++g)
+            if (ready && g < ngroups) {
+#pragma unroll
+              for (int e = 0; e < kSPGroup; e += 4) {
+                const int i = g * kSPGroup + e;
+                const T q0 = buf[(size_t)i * CR], q1 = buf[(size_t)(i + 1) * CR];
+                const T q2 = buf[(size_t)(i + 2) * CR], q3 = buf[(size_t)(i + 3) * CR];
+                if constexpr (kHold) {
+                  qv[i] = q0;
+                  qv[i + 1] = q1;
+                  qv[i + 2] = q2;
+                  qv[i + 3] = q3;
+                }
+                w0 = fma(-q0, s_coef[i], w0);
+                w1 = fma(-q1, s_coef[i + 1], w1);
+                w2 = fma(-q2, s_coef[i + 2], w2);
+                w3 = fma(-q3, s_coef[i + 3], w3);
+              }
+            }
+          w = (w0 + w1) + (w2 + w3);
         }
-        if constexpr (kMode == kStreamProj2) {
+        // rows past the probe's end hold stale shared memory and are left out
+        if (ready && jr < rows) {
+          if constexpr (kUpdate) Wv[b * w_bstride + r0 + jr] = w;
+          if constexpr (kMode == kStreamSubNorm) {
+            const T w2 = w * w;
+            nrm += (double)w2;
+          }
+          if constexpr (kMode == kStreamSub2) {
+            Wo2[b * wo2_bstride + r0 + jr] = w2v;
+            nrm += (double)(w2v * w2v);
+            nrm2 += (double)(w * w);
+            dot2 += (double)(w2v * w);
+          }
+          if constexpr (kMode == kStreamProj2) {
 #pragma unroll
-          for (int g = 0; g < MAXG; ++g)
-            if (g < ngroups) {
+            for (int g = 0; g < MAXG; ++g)
+              if (g < ngroups) {
 #pragma unroll
-              for (int e = 0; e < kSPGroup; ++e) {
-                const int i = g * kSPGroup + e;
-                const T q = buf[(size_t)i * kSR];
-                acc[i] = fma(q, w2v, acc[i]);
-                accg[i] = fma(q, w, accg[i]);
+                for (int e = 0; e < kSPGroup; ++e) {
+                  const int i = g * kSPGroup + e;
+                  const T q = buf[(size_t)i * CR];
+                  acc[i] = fma(q, w2v, acc[i]);
+                  accg[i] = fma(q, w, accg[i]);
+                }
               }
-            }
-          cross = fma(w, w2v, cross);
-        } else if constexpr (kDots) {
+            cross = fma(w, w2v, cross);
+          } else if constexpr (kDots) {
 #pragma unroll
-          for (int g = 0; g < MAXG; ++g)
-            if (g < ngroups) {
+            for (int g = 0; g < MAXG; ++g)
+              if (g < ngroups) {
 #pragma unroll
-              for (int e = 0; e < kSPGroup; ++e) {
-                const int i = g * kSPGroup + e;
-                const T q = kHold ? qv[kHold ? i : 0] : buf[(size_t)i * kSR];
-                acc[i] = fma(q, w, acc[i]);
+                for (int e = 0; e < kSPGroup; ++e) {
+                  const int i = g * kSPGroup + e;
+                  const T q = kHold ? qv[kHold ? i : 0] : buf[(size_t)i * CR];
+                  acc[i] = fma(q, w, acc[i]);
+                }
               }
-            }
+          }
         }
       }
       __syncwarp();
@@ -926,9 +939,9 @@ stream_sweep_kernel(const __grid_constant__ CUtensorMap qmap, const T *__restric
 }
 
 template <typename T>
-static size_t stream_sweep_smem(int ncols, int nbuf, int nv = 1) {
+static size_t stream_sweep_smem(int ncols, int nbuf, int nv = 1, int rpt = 1) {
   const int cpad = (ncols + kSPGroup - 1) / kSPGroup * kSPGroup;
-  return (size_t)nbuf * (cpad + nv) * kSR * sizeof(T) + (size_t)nv * cpad * sizeof(T);
+  return (size_t)nbuf * (cpad + nv) * kSR * rpt * sizeof(T) + (size_t)nv * cpad * sizeof(T);
 }
 
 // Largest vector count of the streamed sweeps: 128 floats, 64 doubles (the
@@ -938,11 +951,11 @@ template <typename T> constexpr int stream_sweep_max_cols() { return sizeof(T) =
 // Ring depth: as many buffers (2..8) as fit in ~110 KB, so that two CTAs
 // share an SM; 0 if the sweep does not apply.
 template <typename T>
-static int stream_sweep_buffers(int ncols, int nv = 1) {
+static int stream_sweep_buffers(int ncols, int nv = 1, int rpt = 1) {
   if (ncols < 1 || ncols > stream_sweep_max_cols<T>()) return 0;
   int nb = kSMaxBuf;
-  while (nb > 2 && stream_sweep_smem<T>(ncols, nb, nv) > 110 * 1024) --nb;
-  return stream_sweep_smem<T>(ncols, nb, nv) <= 220 * 1024 ? nb : 0;
+  while (nb > 2 && stream_sweep_smem<T>(ncols, nb, nv, rpt) > 110 * 1024) --nb;
+  return stream_sweep_smem<T>(ncols, nb, nv, rpt) <= 220 * 1024 ? nb : 0;
 }
 
 struct StreamArgs {
@@ -969,14 +982,14 @@ struct StreamArgs {
   int coff = 0;  // first basis vector of the pass (the vectors are coff .. coff + ncols - 1)
 };
 
-template <typename T, int MAXG, bool kHold, int kMode>
+template <typename T, int MAXG, bool kHold, int kMode, int kRPT = 1>
 static int launch_stream_sweep_t(const StreamArgs &a, cudaStream_t s) {
   constexpr int nv = (kMode == kStreamProj2 || kMode == kStreamSub2) ? 2 : 1;
-  const int nbuf = stream_sweep_buffers<T>(a.ncols, nv);
+  const int nbuf = stream_sweep_buffers<T>(a.ncols, nv, kRPT);
   if (nbuf < 2) return MFG_ERR_UNSUPPORTED;
-  const size_t smem = stream_sweep_smem<T>(a.ncols, nbuf, nv);
+  const size_t smem = stream_sweep_smem<T>(a.ncols, nbuf, nv, kRPT);
   if (a.q_istride <= 0 || a.q_bstride % a.q_istride != 0) return MFG_ERR_BAD_ARG;
-  auto kern = stream_sweep_kernel<T, MAXG, kHold, kMode>;
+  auto kern = stream_sweep_kernel<T, MAXG, kHold, kMode, kRPT>;
   // The default dynamic limit is 48 KB minus the kernel's static shared
   // memory, so the opt-in is raised well below 48 KB.
   if (smem > 32 * 1024)
@@ -999,7 +1012,7 @@ static int launch_stream_sweep_t(const StreamArgs &a, cudaStream_t s) {
   // One wave of CTAs, each with an equal share of the p * C row chunks.  A
   // probe then spans at most ceil(G / p) + 1 CTAs, whose partial sums must
   // fit the workspace's max_fused_chunks(n) slots per probe.
-  const int64_t C = ceil_div(a.n, kSR);
+  const int64_t C = ceil_div(a.n, (int64_t)kSR * kRPT);
   const int64_t F = a.p * C;
   const int64_t cap = max_fused_chunks<T>(a.n);
   int64_t G = (int64_t)sms * per_sm;
@@ -1034,7 +1047,7 @@ static int launch_stream_sweep(const StreamArgs &a, cudaStream_t s) {
       return MFG_ERR_UNSUPPORTED;
     } else {
       if (a.ncols < 1 || a.ncols > kTwoSweepPassCols) return MFG_ERR_UNSUPPORTED;
-      if (a.ncols <= 8) return launch_stream_sweep_t<T, 1, false, kMode>(a, s);
+      if (a.ncols <= 8) return launch_stream_sweep_t<T, 1, false, kMode, 4>(a, s);
       if (a.ncols <= 32) return launch_stream_sweep_t<T, 4, false, kMode>(a, s);
       return launch_stream_sweep_t<T, 8, false, kMode>(a, s);
     }
