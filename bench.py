@@ -816,7 +816,14 @@ def serve_arm(args):
     srv.run(warm, realtime=False)
     torch.cuda.synchronize()
     with ClockSampler(0) as clk:
-        res, stats = srv.run(reqs, realtime=True)
+        try:
+            res, stats = srv.run(reqs, realtime=True, stall_s=args.stall_s)
+        except RuntimeError as exc:
+            print(json.dumps({"metric": METRIC, "value": None, "unit": UNIT, "n_gpus": 1,
+                              "error": f"serving stalled: {exc}"}), flush=True)
+            # leave without the interpreter's exit handlers, which would wait
+            # for the solves that did not finish
+            os._exit(3)
     clocks = clk.summary()
     by_id = {r.rid: r for r in res}
     # plain per-request FP32 (cuBLAS SGEMM, TF32 off) on a prefix of the stream
@@ -896,6 +903,9 @@ def run_other_configs(timeout_s=900):
             lines = [ln for ln in proc.stdout.splitlines() if ln.startswith("{")]
             if proc.returncode == 0 and lines:
                 out[name] = json.loads(lines[-1])
+            elif lines:  # a failure the arm reported itself (e.g. a serving stall)
+                out[name] = json.loads(lines[-1])
+                out[name]["rc"] = proc.returncode
             else:
                 out[name] = {"error": f"rc {proc.returncode}", "stderr_tail": proc.stderr[-2000:]}
         except subprocess.TimeoutExpired:
@@ -923,6 +933,8 @@ def main():
     ap.add_argument("--precision", default="bf16x3", choices=["fp32", "bf16", "bf16x3", "fp64"])
     ap.add_argument("--cpu-probes", type=int, default=8)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--stall-s", type=float, default=60.0,
+                    help="serve config: give up when no solve completes for this many seconds")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the built-in tensor-core tile configuration")
     ap.add_argument("--no-other-configs", action="store_true",

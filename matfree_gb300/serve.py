@@ -340,15 +340,30 @@ class SLQServer:
         pending.extend(rest)
         return group
 
-    def run(self, requests, *, realtime: bool = True):
-        """Serve the requests in arrival order; returns (results, stats)."""
+    def run(self, requests, *, realtime: bool = True, stall_s: float | None = None):
+        """Serve the requests in arrival order; returns (results, stats).
+
+        stall_s: if solves are in flight and none completes for this many
+        seconds, raise RuntimeError describing the solves in flight (a solve
+        that does not finish would otherwise keep the loop polling forever).
+        """
         pending = deque(sorted(requests, key=lambda r: r.arrival))
         packs = [0, 0]  # packed solves, requests in them
         inflight = {}
         results = []
         t0 = time.perf_counter()
+        last_progress = t0
         while pending or inflight:
             now = time.perf_counter() - t0
+            if stall_s is not None and inflight and time.perf_counter() - last_progress > stall_s:
+                desc = []
+                for idx, (slot, req, st, fp, t_start) in inflight.items():
+                    members = st.get("group", [req])
+                    desc.append({"rid": req.rid, "members": [(r.rid, r.x.shape[0], r.k, r.p) for r in members],
+                                 "flags": st["flags"], "slot": self.slots.index(slot),
+                                 "age_s": round(now - t_start, 3)})
+                raise RuntimeError(f"no solve completed for {stall_s} s; in flight: {desc}; "
+                                   f"{len(results)} done, {len(pending)} pending")
             for idx, (slot, req, st, fp, t_start) in list(inflight.items()):
                 if st["done"].query() and st["flags"] and _lib.lib().mfg_workspace_status(
                         st["ws"], ctypes.c_void_p(slot.stream.cuda_stream)) == _lib.MFG_ERR_RETRY:
@@ -368,6 +383,7 @@ class SLQServer:
                     slot.busy = False
                     self.used -= fp
                     del inflight[idx]
+                    last_progress = time.perf_counter()
             admitted = False
             while pending and (not realtime or pending[0].arrival <= now):
                 req = pending[0]
