@@ -37,6 +37,9 @@ from oracle import philox, problems, slq
 
 pytestmark = pytest.mark.gpu
 
+# a solve that does not finish fails the test instead of blocking the suite
+STALL_S = 120.0
+
 DEV = "cuda"
 
 
@@ -191,7 +194,7 @@ def test_serving_stream_requests_match_oracle():
     for r in chosen:
         r.arrival = 0.0
     assert max(r.x.shape[0] for r in chosen) > 32000
-    results, stats = serve.SLQServer(slots=4).run(chosen, realtime=False)
+    results, stats = serve.SLQServer(slots=4).run(chosen, realtime=False, stall_s=STALL_S)
     assert stats["solves"] == len(chosen)
     by_id = {res.rid: res for res in results}
     for r in chosen:

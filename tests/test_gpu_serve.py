@@ -8,6 +8,9 @@ from oracle import philox, problems, slq
 
 pytestmark = pytest.mark.gpu
 
+# a solve that does not finish fails the test instead of blocking the suite
+STALL_S = 120.0
+
 
 def _requests(num=6, seed=3):
     reqs = serve.synthetic_stream(num, rate=1e6, seed=seed, n_range=(512, 2048), ks=(16, 24),
@@ -22,9 +25,9 @@ def test_result_is_identical_alone_and_in_the_mix():
     reqs = _requests()
     alone = []
     for r in reqs:
-        res, _ = serve.SLQServer(slots=1, group_max_n=0).run([r], realtime=False)
+        res, _ = serve.SLQServer(slots=1, group_max_n=0).run([r], realtime=False, stall_s=STALL_S)
         alone.append(res[0])
-    mixed, stats = serve.SLQServer(slots=4, group_max_n=0).run(reqs, realtime=False)
+    mixed, stats = serve.SLQServer(slots=4, group_max_n=0).run(reqs, realtime=False, stall_s=STALL_S)
     assert stats["solves"] == len(reqs) and stats["packed_solves"] == 0
     for a, m in zip(alone, mixed):
         assert a.rid == m.rid
@@ -41,9 +44,9 @@ def test_packed_requests_match_their_alone_values():
         r.arrival = 0.0
     alone = {}
     for r in reqs:
-        res, _ = serve.SLQServer(slots=1, group_max_n=0).run([r], realtime=False)
+        res, _ = serve.SLQServer(slots=1, group_max_n=0).run([r], realtime=False, stall_s=STALL_S)
         alone[r.rid] = res[0]
-    packed, stats = serve.SLQServer(slots=2).run(reqs, realtime=False)
+    packed, stats = serve.SLQServer(slots=2).run(reqs, realtime=False, stall_s=STALL_S)
     assert stats["solves"] == len(reqs)
     assert stats["packed_solves"] >= 1 and stats["packed_requests"] >= 4
     for m in packed:
@@ -58,7 +61,7 @@ def test_packed_group_matches_oracle(fun):
                                   funs=(fun,))
     for r in reqs:
         r.arrival = 0.0
-    res, stats = serve.SLQServer(slots=1).run(reqs, realtime=False)
+    res, stats = serve.SLQServer(slots=1).run(reqs, realtime=False, stall_s=STALL_S)
     assert stats["packed_requests"] == len(reqs)
     f = np.log if fun == "log" else (lambda t: np.exp(-0.1 * t))
     for r, got in zip(reqs, res):
@@ -82,11 +85,11 @@ def test_admission_respects_the_memory_budget():
         return orig(slot, req)
 
     server._launch = spy
-    res, stats = server.run(reqs, realtime=False)
+    res, stats = server.run(reqs, realtime=False, stall_s=STALL_S)
     assert stats["solves"] == len(reqs)
     assert max(seen) <= 1.5 * biggest
     with pytest.raises(ValueError, match="budget"):
-        serve.SLQServer(slots=1, budget_bytes=biggest / 10, group_max_n=0).run(reqs[:1], realtime=False)
+        serve.SLQServer(slots=1, budget_bytes=biggest / 10, group_max_n=0).run(reqs[:1], realtime=False, stall_s=STALL_S)
 
 
 @pytest.mark.parametrize("fun", ["log", "exp:-0.1"])
@@ -94,7 +97,7 @@ def test_served_value_matches_oracle(fun):
     n, k, p = 1024, 24, 32
     x = problems.rbf_points(n, seed=9).astype(np.float32)
     req = serve.Request(rid=0, x=x, k=k, p=p, fun=fun, key=(7, 0))
-    (res,), _ = serve.SLQServer(slots=1).run([req], realtime=False)
+    (res,), _ = serve.SLQServer(slots=1).run([req], realtime=False, stall_s=STALL_S)
     K = problems.rbf_kernel(x.astype(np.float64))
     V = philox.rademacher(np.array([7, 0], dtype=np.uint32), p, n)
     f = np.log if fun == "log" else (lambda t: np.exp(-0.1 * t))
