@@ -813,7 +813,7 @@ def serve_arm(args):
     reqs = serve.synthetic_stream(args.requests, rate=args.rate, seed=0)
     warm = serve.synthetic_stream(8, rate=1e6, seed=99)
     srv = serve.SLQServer(slots=args.slots, budget_bytes=150e9, precision="bf16x3", autotune=True)
-    srv.run(warm, realtime=False)
+    srv.run(warm, realtime=False, stall_s=args.stall_s)
     torch.cuda.synchronize()
     with ClockSampler(0) as clk:
         try:
