@@ -813,17 +813,23 @@ def serve_arm(args):
     reqs = serve.synthetic_stream(args.requests, rate=args.rate, seed=0)
     warm = serve.synthetic_stream(8, rate=1e6, seed=99)
     srv = serve.SLQServer(slots=args.slots, budget_bytes=150e9, precision="bf16x3", autotune=True)
-    srv.run(warm, realtime=False, stall_s=args.stall_s)
+    def stalled(exc):
+        print(json.dumps({"metric": METRIC, "value": None, "unit": UNIT, "n_gpus": 1,
+                          "error": f"serving stalled: {exc}"}), flush=True)
+        # leave without the interpreter's exit handlers, which would wait for
+        # the solves that did not finish
+        os._exit(3)
+
+    try:
+        srv.run(warm, realtime=False, stall_s=args.stall_s)
+    except RuntimeError as exc:
+        stalled(exc)
     torch.cuda.synchronize()
     with ClockSampler(0) as clk:
         try:
             res, stats = srv.run(reqs, realtime=True, stall_s=args.stall_s)
         except RuntimeError as exc:
-            print(json.dumps({"metric": METRIC, "value": None, "unit": UNIT, "n_gpus": 1,
-                              "error": f"serving stalled: {exc}"}), flush=True)
-            # leave without the interpreter's exit handlers, which would wait
-            # for the solves that did not finish
-            os._exit(3)
+            stalled(exc)
     clocks = clk.summary()
     by_id = {r.rid: r for r in res}
     # plain per-request FP32 (cuBLAS SGEMM, TF32 off) on a prefix of the stream
