@@ -829,6 +829,7 @@ def serve_arm(args):
         try:
             res, stats = srv.run(reqs, realtime=True, stall_s=args.stall_s)
         except RuntimeError as exc:
+            clk.__exit__(None, None, None)  # stop the clock sampler's nvidia-smi first
             stalled(exc)
     clocks = clk.summary()
     by_id = {r.rid: r for r in res}
