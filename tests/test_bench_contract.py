@@ -37,3 +37,14 @@ def test_reference_arm_other_ranks_exit_quietly():
     out = _run({"RANK": "1"})
     assert out.returncode == 0, out.stderr
     assert out.stdout.strip() == ""
+
+
+def test_reference_arm_stops_timing_at_its_budget():
+    # every timed step is a complete solve; past the budget no further step runs
+    out = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--config", "dense1k",
+                          "--steps", "3", "--warmup", "3", "--reference-budget-s", "0"],
+                         cwd=ROOT, capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr
+    line = json.loads(out.stdout.strip().splitlines()[-1])
+    assert line["steps"] == 1 and line["steps_requested"] == 3
+    assert abs(line["value"] - 1e3 / line["ms_per_step"]) <= 1e-9 * line["value"]
