@@ -55,6 +55,19 @@ def _time_apply(op_struct, panel, out, p, ld, ws, reps):
     return best
 
 
+def pick(timings, margin: float = None):
+    """(default_ms, (ms, bn, split)) from [(ms, bn, split), ...] that holds
+    the built-in choice (0, 0): the fastest candidate, unless it is within
+    `margin` of the built-in one, which then stays (it keeps the launch chain
+    free of extra operations such as the zeroing before a K split)."""
+    margin = MARGIN if margin is None else margin
+    default_ms = next(t for t, b, sp in timings if b == 0 and sp == 0)
+    best = min(timings)
+    if best[0] > default_ms * (1.0 - margin):
+        best = (default_ms, 0, 0)
+    return default_ms, best
+
+
 def _bounds(values, i):
     """Half-open log-midpoint range around values[i] (the rule's n or p range)."""
     lo = 0 if i == 0 else int(math.sqrt(values[i - 1] * values[i])) + 1
@@ -93,12 +106,7 @@ def autotune(ns=DEFAULT_NS, ps=DEFAULT_PS, precision: str = "bf16x3", reps: int 
                 lib.mfg_gemm_tuning_clear()
                 _lib.check(lib.mfg_gemm_tuning_add(n, n, p, p, bn, split), "mfg_gemm_tuning_add")
                 timings.append((_time_apply(s, panel, out, p, ld, ws.buf, reps), bn, split))
-            default_ms = next(t for t, b, sp in timings if b == 0 and sp == 0)
-            ms, bn, split = min(timings)
-            if ms > default_ms * (1.0 - MARGIN):
-                # within timing noise of the built-in choice, which keeps the
-                # launch chain free of extra operations
-                ms, bn, split = default_ms, 0, 0
+            default_ms, (ms, bn, split) = pick(timings)
             n_lo, n_hi = _bounds(ns, i)
             p_lo, p_hi = _bounds(ps, j)
             rules.append({"n_lo": n_lo, "n_hi": n_hi, "p_lo": p_lo, "p_hi": p_hi, "bn": bn,

@@ -243,6 +243,19 @@ def test_tuning_rule_ranges_tile_the_axis():
         assert lo == hi + 1
 
 
+def test_tuning_keeps_the_built_in_form_within_the_margin():
+    from matfree_gb300 import tuning
+
+    # (ms, bn, split); the built-in choice is (0, 0)
+    base = [(1.00, 0, 0), (0.99, 0, 3), (1.20, 128, 1)]
+    assert tuning.pick(base, margin=0.03) == (1.00, (1.00, 0, 0))  # 1 % faster: noise
+    faster = [(1.00, 0, 0), (0.95, 0, 2), (0.96, 128, 3)]
+    assert tuning.pick(faster, margin=0.03) == (1.00, (0.95, 0, 2))
+    assert tuning.pick(faster, margin=0.10) == (1.00, (1.00, 0, 0))
+    slower = [(1.00, 0, 0), (1.10, 64, 1)]
+    assert tuning.pick(slower) == (1.00, (1.00, 0, 0))
+
+
 def test_gemm_tuning_rejects_bad_rules():
     lib = _lib.lib()
     assert lib.mfg_gemm_tuning_add(1024, 2048, 64, 64, 48, 0) == _lib.MFG_ERR_BAD_ARG  # not a multiple of 32
