@@ -48,3 +48,22 @@ def test_reference_arm_stops_timing_at_its_budget():
     line = json.loads(out.stdout.strip().splitlines()[-1])
     assert line["steps"] == 1 and line["steps_requested"] == 3
     assert abs(line["value"] - 1e3 / line["ms_per_step"]) <= 1e-9 * line["value"]
+
+
+def test_roofline_of_fma_pipe_products():
+    # fp32 / fp64 products are bounded by the FMA pipes, not the tensor cores
+    sys.path.insert(0, ROOT)
+    import bench
+
+    prof = {c: {"ms": 0.0, "bytes": 0.0, "flops": 0.0, "launches": 0}
+            for c in ("apply", "proj", "subproj", "sub", "scale", "quad", "other")}
+    prof["apply"] = {"ms": 10.0, "bytes": 0.0, "flops": 7.2e9, "launches": 10}
+    peaks = {"hbm": 6668.2, "tensor_burst": 1932.3, "tensor_sustained": 1729.1, "source": "measured"}
+    rl = bench.roofline(prof, peaks, 1, "dense1k", "fp64")
+    assert rl["bound"] == "fp64 fma" and rl["peak"] == 1.25
+    assert abs(rl["achieved"] - 0.72) < 1e-9 and abs(rl["frac"] - 0.72 / 1.25) < 1e-12
+    assert "nominal" in rl["peak_override"]
+    rl32 = bench.roofline(prof, peaks, 1, "dense1k", "fp32")
+    assert rl32["bound"] == "fp32 fma" and abs(rl32["peak"] - 152 * 256 * 2.07e9 / 1e12) < 1e-9
+    rlt = bench.roofline(prof, peaks, 1, "rbf16k", "bf16x3")
+    assert rlt["bound"] == "tensor" and rlt["peak"] == 1932.3
